@@ -1,0 +1,242 @@
+"""ctypes binding of libffg (include/ffg.h).
+
+The library is built in-tree by ``fastfermion_gb300._build``.  There is no CPU
+fallback: when the library cannot be loaded or no CUDA device is present the
+calls raise.
+"""
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import _build
+
+PAULI_GATE = np.dtype([("kind", "<i4"), ("q0", "<i4"), ("q1", "<i4"), ("pad", "<i4"),
+                       ("x", "<u8", (2,)), ("z", "<u8", (2,)), ("theta", "<f8")])
+MAJORANA_GATE = np.dtype([("alpha", "<u8", (4,)), ("theta", "<f8"), ("r", "<i4"), ("pad", "<i4")])
+ROT, H, S, CNOT, SWAP, CZ = range(6)
+
+
+class PauliParams(ctypes.Structure):
+    _fields_ = [("maxdegree", ctypes.c_int32), ("topk", ctypes.c_int32),
+                ("mincoeff", ctypes.c_double), ("max_xweight", ctypes.c_int32),
+                ("xtrunc_period", ctypes.c_int32), ("batched", ctypes.c_int32),
+                ("deterministic", ctypes.c_int32)]
+
+
+class MajoranaParams(ctypes.Structure):
+    _fields_ = [("has_maxdegree", ctypes.c_int32), ("maxdegree", ctypes.c_int32),
+                ("mincoeff", ctypes.c_double), ("deterministic", ctypes.c_int32),
+                ("pad", ctypes.c_int32)]
+
+
+class Profile(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in (
+        "seconds_total", "seconds_rotations", "seconds_truncate", "seconds_clifford",
+        "seconds_compact", "seconds_h2d", "seconds_d2h")] + [
+        (n, ctypes.c_int64) for n in (
+            "n_gates", "apps", "emits", "peak_terms", "final_terms", "syncs", "regrows", "compactions",
+            "kernel_launches")]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_lib = None
+_lock = threading.Lock()
+
+EXPORTS = ["ffg_create", "ffg_destroy", "ffg_last_error", "ffg_set_profiling", "ffg_profile_get",
+           "ffg_pauli_propagate", "ffg_majorana_propagate", "ffg_result_size", "ffg_result_kind",
+           "ffg_result_copy", "ffg_result_device", "ffg_result_overlapwithzero",
+           "ffg_result_qubit_state", "ffg_result_fock_state", "ffg_result_free", "ffg_abs_le",
+           "ffg_pauli_schedule", "ffg_stream"]
+
+
+def lib():
+    """Loads libffg.so (building it first when the sources are newer)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            L = ctypes.CDLL(path)
+            vp, sz, i32, i64 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int32, ctypes.c_int64
+            dp = ctypes.POINTER(ctypes.c_double)
+            L.ffg_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int]
+            L.ffg_destroy.argtypes = [vp]
+            L.ffg_last_error.restype = ctypes.c_char_p
+            L.ffg_last_error.argtypes = [vp]
+            L.ffg_set_profiling.argtypes = [vp, ctypes.c_int]
+            L.ffg_profile_get.argtypes = [vp, ctypes.POINTER(Profile)]
+            L.ffg_pauli_propagate.argtypes = [vp, vp, vp, vp, sz, vp, sz, ctypes.POINTER(PauliParams),
+                                              ctypes.c_int, ctypes.POINTER(vp)]
+            L.ffg_majorana_propagate.argtypes = [vp, vp, vp, vp, sz, vp, sz,
+                                                 ctypes.POINTER(MajoranaParams), ctypes.c_int,
+                                                 ctypes.POINTER(vp)]
+            L.ffg_result_size.restype = sz
+            L.ffg_result_size.argtypes = [vp]
+            L.ffg_result_kind.argtypes = [vp]
+            L.ffg_result_copy.argtypes = [vp, vp, vp, vp]
+            L.ffg_result_device.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(sz),
+                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(vp),
+                                            ctypes.POINTER(vp)]
+            L.ffg_result_overlapwithzero.argtypes = [vp, dp, dp]
+            L.ffg_result_qubit_state.argtypes = [vp, vp, dp, dp]
+            L.ffg_result_fock_state.argtypes = [vp, vp, dp, dp]
+            L.ffg_result_free.argtypes = [vp]
+            L.ffg_abs_le.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double]
+            L.ffg_stream.restype = vp
+            L.ffg_stream.argtypes = [vp]
+            L.ffg_pauli_schedule.restype = i64
+            L.ffg_pauli_schedule.argtypes = [vp, sz, ctypes.c_int, vp, i64]
+            _lib = L
+    return _lib
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    return ctypes.c_void_p(a.ctypes.data) if a.size else None
+
+
+class FFGError(RuntimeError):
+    pass
+
+
+class Context:
+    """One libffg context (one CUDA stream on one device)."""
+
+    def __init__(self, device=0):
+        self.L = lib()
+        self.h = ctypes.c_void_p()
+        rc = self.L.ffg_create(ctypes.byref(self.h), int(device))
+        if rc != 0:
+            raise FFGError(f"ffg_create failed ({rc}): no usable CUDA device {device}")
+        self.device = device
+
+    def check(self, rc):
+        if rc != 0:
+            msg = self.L.ffg_last_error(self.h).decode()
+            if rc == -1:
+                raise RuntimeError(msg)
+            raise FFGError(f"libffg error {rc}: {msg}")
+
+    def stream(self):
+        """cudaStream_t of the context (integer handle)."""
+        return self.L.ffg_stream(self.h) or 0
+
+    def set_profiling(self, on):
+        self.check(self.L.ffg_set_profiling(self.h, int(bool(on))))
+
+    def profile(self):
+        p = Profile()
+        self.check(self.L.ffg_profile_get(self.h, ctypes.byref(p)))
+        return p.as_dict()
+
+    def pauli_propagate(self, keys, re, im, gates, params, on_device=False):
+        """keys: uint64 (4, n); re, im: float64 (n,); gates: PAULI_GATE array.
+        With on_device, keys/re/im are integer device addresses instead."""
+        out = ctypes.c_void_p()
+        if on_device:
+            kp, rp, ip, n = keys, re, im, params.pop("n")
+        else:
+            keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
+            re = np.ascontiguousarray(re, dtype=np.float64)
+            im = None if im is None else np.ascontiguousarray(im, dtype=np.float64)
+            kp, rp, ip, n = _ptr(keys), _ptr(re), _ptr(im), re.size
+        gates = np.ascontiguousarray(gates, dtype=PAULI_GATE)
+        p = PauliParams(**params)
+        self.check(self.L.ffg_pauli_propagate(self.h, kp, rp, ip, n, _ptr(gates), gates.size,
+                                              ctypes.byref(p), int(bool(on_device)),
+                                              ctypes.byref(out)))
+        return Result(self, out)
+
+    def majorana_propagate(self, keys, re, im, gates, params):
+        out = ctypes.c_void_p()
+        keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
+        re = np.ascontiguousarray(re, dtype=np.float64)
+        im = None if im is None else np.ascontiguousarray(im, dtype=np.float64)
+        gates = np.ascontiguousarray(gates, dtype=MAJORANA_GATE)
+        p = MajoranaParams(**params)
+        self.check(self.L.ffg_majorana_propagate(self.h, _ptr(keys), _ptr(re), _ptr(im), re.size,
+                                                 _ptr(gates), gates.size, ctypes.byref(p), 0,
+                                                 ctypes.byref(out)))
+        return Result(self, out)
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.ffg_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+
+class Result:
+    """A propagated polynomial held in device memory."""
+
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self.h = handle
+        self.n = ctx.L.ffg_result_size(handle)
+        self.kind = ctx.L.ffg_result_kind(handle)
+
+    def copy(self):
+        keys = np.zeros((4, self.n), dtype=np.uint64)
+        re = np.zeros(self.n)
+        im = np.zeros(self.n)
+        if self.n:
+            self.ctx.check(self.ctx.L.ffg_result_copy(self.h, _ptr(keys), _ptr(re), _ptr(im)))
+        return keys, re, im
+
+    def _pair(self, fn, *args):
+        r, i = ctypes.c_double(), ctypes.c_double()
+        self.ctx.check(fn(self.h, *args, ctypes.byref(r), ctypes.byref(i)))
+        return complex(r.value, i.value)
+
+    def overlapwithzero(self):
+        return self._pair(self.ctx.L.ffg_result_overlapwithzero)
+
+    def qubit_state(self, b0=0, b1=0):
+        b = np.array([b0, b1], dtype=np.uint64)
+        return self._pair(self.ctx.L.ffg_result_qubit_state, _ptr(b))
+
+    def fock_state(self, b0=0, b1=0):
+        b = np.array([b0, b1], dtype=np.uint64)
+        return self._pair(self.ctx.L.ffg_result_fock_state, _ptr(b))
+
+    def free(self):
+        if self.h is not None and self.h.value:
+            self.ctx.L.ffg_result_free(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+_contexts = {}
+
+
+def context(device=None):
+    """The process-wide context of a device (created on first use)."""
+    if device is None:
+        device = int(os.environ.get("FFG_DEVICE", "0"))
+    with _lock:
+        ctx = _contexts.get(device)
+    if ctx is None:
+        ctx = Context(device)
+        with _lock:
+            _contexts[device] = ctx
+    return ctx
+
+
+def abs_le(re, im, tau):
+    return bool(lib().ffg_abs_le(float(re), float(im), float(tau)))
+
+
+def pauli_schedule(gates, batched=True):
+    gates = np.ascontiguousarray(gates, dtype=PAULI_GATE)
+    cap = max(gates.size, 1)
+    sizes = np.zeros(cap, dtype=np.int64)
+    nb = lib().ffg_pauli_schedule(_ptr(gates), gates.size, int(bool(batched)), _ptr(sizes), cap)
+    return sizes[:nb].tolist()

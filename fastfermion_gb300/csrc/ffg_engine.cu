@@ -1,0 +1,1118 @@
+// Host engine of libffg: term-store memory, the propagation schedule and the
+// C ABI declared in include/ffg.h.
+//
+// Schedule (src/pauli/propagate.h:297-493): the circuit is walked last gate
+// first; consecutive Clifford gates form a segment applied term by term;
+// rotations are buffered and split greedily into maximal runs of mutually
+// commuting axes (batch_commuting_gates, :272-291); truncation runs after each
+// run (batched) or after each rotation (unbatched) with the reference's
+// rot_count bookkeeping for the X-weight period.  Majorana circuits apply
+// every gate last to first with a threshold after each gate
+// (src/majorana_propagation.h:18-33).
+//
+// The schedule is turned into a flat op list once; ops are enqueued on the
+// context stream in chunks without host round trips (kernels agree on the
+// store size through device counters).  After each chunk the host reads the
+// counters once: a rotation that found the store too small set the overflow
+// flag and every later op of the chunk skipped itself, so the host grows the
+// store and replays from that op.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ffg.h"
+#include "ffg_kernels.cuh"
+
+using namespace ffg;
+
+namespace {
+
+struct RawBuf {
+    char* p = nullptr;
+    size_t bytes = 0;
+};
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+size_t store_bytes(int kw, bool cplx, u64 cap) {
+    size_t b = align256((size_t)kw * cap * 8);
+    b += align256(cap * 8);
+    if (cplx) b += align256(cap * 8);
+    b += align256(cap);
+    b += align256(2 * cap * 8);                      // index slots (load <= 1/2)
+    b += align256((cap / kTileItems + 2) * 8);       // compaction tile offsets
+    return b;
+}
+
+struct Store {
+    StoreView v{};
+    u64* tiles = nullptr;
+    RawBuf* buf = nullptr;
+};
+
+Store carve(RawBuf& rb, int kw, bool cplx, u64 cap) {
+    Store s;
+    char* p = rb.p;
+    s.v.cap = cap;
+    s.v.key = (u64*)p;
+    p += align256((size_t)kw * cap * 8);
+    s.v.re = (double*)p;
+    p += align256(cap * 8);
+    s.v.im = nullptr;
+    if (cplx) {
+        s.v.im = (double*)p;
+        p += align256(cap * 8);
+    }
+    s.v.dead = (unsigned char*)p;
+    p += align256(cap);
+    s.v.slots = (u64*)p;
+    s.v.hmask = 2 * cap - 1;
+    p += align256(2 * cap * 8);
+    s.tiles = (u64*)p;
+    s.buf = &rb;
+    return s;
+}
+
+u64 pow2_at_least(u64 x) {
+    u64 c = 1;
+    while (c < x) c <<= 1;
+    return c;
+}
+
+int popc64(u64 x) { return __builtin_popcountll(x); }
+
+struct Op {
+    enum Type { ROT, TRUNC, CLIFF } type;
+    int idx;     // ROT: index into rot args; TRUNC: index into trunc args
+    int begin;   // CLIFF: circuit range [begin, end)
+    int end;
+    int topk;    // TRUNC: top-k after threshold/x-weight
+};
+
+struct PendingEvent {
+    cudaEvent_t a, b;
+    int phase;
+};
+
+}  // namespace
+
+struct ffg_ctx {
+    int device = 0;
+    int num_sms = 152;
+    cudaStream_t stream = nullptr;
+    DevCounters* d_ctr = nullptr;
+    DevCounters* h_ctr = nullptr;  // pinned
+    RawBuf buf[2];
+    CliffordOp* d_cliff = nullptr;
+    size_t cliff_cap = 0;
+    double* d_part = nullptr;  // expectation partial sums (2 * kMaxParts)
+    u64* d_hist = nullptr;     // 256 bins
+    u64* d_ties = nullptr;
+    size_t ties_cap = 0;
+    std::string err;
+    bool profiling = false;
+    ffg_profile prof{};
+    std::vector<PendingEvent> events;
+    std::vector<cudaEvent_t> free_events;
+};
+
+struct ffg_result {
+    int kind = 1;   // 1 Pauli, 2 Majorana
+    int nplanes = 4;
+    bool cplx = false;
+    bool deterministic = false;
+    size_t n = 0;
+    int device = 0;
+    u64* key = nullptr;   // nplanes * n
+    double* re = nullptr;
+    double* im = nullptr;
+    unsigned char* dead = nullptr;  // zeros (lets the reduction kernels share the store view)
+    ffg_ctx* ctx = nullptr;
+};
+
+namespace {
+
+constexpr int kMaxParts = 1024;
+constexpr int kChunkOps = 128;
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                \
+            return FFG_ERR_CUDA;                                                          \
+        }                                                                                 \
+    } while (0)
+
+int set_err(ffg_ctx* ctx, int code, const std::string& m) {
+    ctx->err = m;
+    return code;
+}
+
+int ensure_buf(ffg_ctx* ctx, RawBuf& rb, size_t bytes) {
+    if (rb.bytes >= bytes) return FFG_OK;
+    if (rb.p) CK(cudaFree(rb.p));
+    rb.p = nullptr;
+    rb.bytes = 0;
+    CK(cudaMalloc(&rb.p, bytes));
+    rb.bytes = bytes;
+    return FFG_OK;
+}
+
+int grid_for(const ffg_ctx* ctx, u64 items) {
+    u64 b = (items + kBlock - 1) / kBlock;
+    u64 lim = (u64)ctx->num_sms * 4;
+    if (b < 1) b = 1;
+    return (int)std::min(b, lim);
+}
+
+// ---------------------------------------------------------------------------
+// profiling events
+// ---------------------------------------------------------------------------
+enum { PH_ROT = 0, PH_TRUNC, PH_CLIFF, PH_COMPACT };
+
+cudaEvent_t get_event(ffg_ctx* ctx) {
+    if (!ctx->free_events.empty()) {
+        cudaEvent_t e = ctx->free_events.back();
+        ctx->free_events.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+struct PhaseScope {
+    ffg_ctx* ctx;
+    int phase;
+    cudaEvent_t a{}, b{};
+    PhaseScope(ffg_ctx* c, int ph) : ctx(c), phase(ph) {
+        if (ctx->profiling) {
+            a = get_event(ctx);
+            cudaEventRecord(a, ctx->stream);
+        }
+    }
+    ~PhaseScope() {
+        if (ctx->profiling) {
+            b = get_event(ctx);
+            cudaEventRecord(b, ctx->stream);
+            ctx->events.push_back({a, b, phase});
+        }
+    }
+};
+
+void drain_events(ffg_ctx* ctx) {
+    for (auto& e : ctx->events) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e.a, e.b);
+        double s = ms * 1e-3;
+        switch (e.phase) {
+            case PH_ROT: ctx->prof.seconds_rotations += s; break;
+            case PH_TRUNC: ctx->prof.seconds_truncate += s; break;
+            case PH_CLIFF: ctx->prof.seconds_clifford += s; break;
+            default: ctx->prof.seconds_compact += s; break;
+        }
+        ctx->free_events.push_back(e.a);
+        ctx->free_events.push_back(e.b);
+    }
+    ctx->events.clear();
+}
+
+// ---------------------------------------------------------------------------
+// Engine: one term store layout (KW key planes, real or complex coefficients)
+// ---------------------------------------------------------------------------
+template <int KW, bool CPLX, bool PAULI>
+struct Engine {
+    static constexpr int NW = PAULI ? KW / 2 : 0;
+    ffg_ctx* ctx;
+    int active = 0;  // which RawBuf holds the live store
+    Store cur;
+    u64 cap = 0;
+
+    explicit Engine(ffg_ctx* c) : ctx(c) {}
+
+    int sync_counters() {
+        CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        ctx->prof.syncs++;
+        if (ctx->profiling) drain_events(ctx);
+        if (ctx->h_ctr->error & 1u) return set_err(ctx, FFG_ERR_ARG, "input contains duplicate keys");
+        if (ctx->h_ctr->error) return set_err(ctx, FFG_ERR_STATE, "term-store index probe overrun");
+        return FFG_OK;
+    }
+
+    void reindex(Store& s, int check_dup) {
+        const u64 nslots = s.v.hmask + 1;
+        clear_slots_kernel<<<grid_for(ctx, nslots), kBlock, 0, ctx->stream>>>(s.v.slots, nslots);
+        index_kernel<KW><<<grid_for(ctx, s.v.cap), kBlock, 0, ctx->stream>>>(s.v, ctx->d_ctr, check_dup);
+        ctx->prof.kernel_launches += 2;
+    }
+
+    // order-preserving compaction of live entries into buffer `to` (capacity newcap)
+    int compact_into(int to, u64 newcap) {
+        PhaseScope ps(ctx, PH_COMPACT);
+        int rc = ensure_buf(ctx, ctx->buf[to], store_bytes(KW, CPLX, newcap));
+        if (rc) return rc;
+        Store dst = carve(ctx->buf[to], KW, CPLX, newcap);
+        const u64 ntiles = (cap + kTileItems - 1) / kTileItems;
+        const int g = (int)std::min<u64>(std::max<u64>(ntiles, 1), (u64)ctx->num_sms * 8);
+        tile_count_kernel<<<g, kBlock, 0, ctx->stream>>>(cur.v, ctx->d_ctr, cur.tiles);
+        tile_scan_kernel<<<1, 1024, 0, ctx->stream>>>(ctx->d_ctr, cur.tiles);
+        scatter_kernel<KW, CPLX><<<g, kBlock, 0, ctx->stream>>>(cur.v, dst.v, ctx->d_ctr, cur.tiles);
+        compact_commit_kernel<<<1, 1, 0, ctx->stream>>>(ctx->d_ctr, cur.tiles);
+        ctx->prof.kernel_launches += 4;
+        cur = dst;
+        cap = newcap;
+        active = to;
+        reindex(cur, 0);
+        ctx->prof.compactions++;
+        CK(cudaGetLastError());
+        return FFG_OK;
+    }
+
+    int load(const uint64_t* keys, const double* re, const double* im, size_t n, int on_device,
+             int pauli_nw_in /* planes layout of the caller: 4 planes */) {
+        (void)pauli_nw_in;
+        cap = pow2_at_least(std::max<u64>((u64)n * 4, 1u << 16));
+        int rc = ensure_buf(ctx, ctx->buf[0], store_bytes(KW, CPLX, cap));
+        if (rc) return rc;
+        active = 0;
+        cur = carve(ctx->buf[0], KW, CPLX, cap);
+        auto t0 = std::chrono::steady_clock::now();
+        const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+        if (n) {
+            for (int w = 0; w < KW; w++) {
+                // caller plane for store plane w
+                int src = w;
+                if (PAULI) src = (w < NW) ? w : 2 + (w - NW);
+                CK(cudaMemcpyAsync(cur.v.key + (size_t)w * cap, keys + (size_t)src * n, n * 8, kind,
+                                   ctx->stream));
+            }
+            CK(cudaMemcpyAsync(cur.v.re, re, n * 8, kind, ctx->stream));
+            if (CPLX) {
+                if (im)
+                    CK(cudaMemcpyAsync(cur.v.im, im, n * 8, kind, ctx->stream));
+                else
+                    CK(cudaMemsetAsync(cur.v.im, 0, n * 8, ctx->stream));
+            }
+        }
+        CK(cudaMemsetAsync(cur.v.dead, 0, cap, ctx->stream));
+        DevCounters h{};
+        h.n = n;
+        h.alive = n;
+        h.peak = n;
+        *ctx->h_ctr = h;
+        CK(cudaMemcpyAsync(ctx->d_ctr, ctx->h_ctr, sizeof(DevCounters), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        reindex(cur, 1);
+        rc = sync_counters();
+        ctx->prof.seconds_h2d += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return rc;
+    }
+
+    void launch_rot(const RotArgs& a) {
+        PhaseScope ps(ctx, PH_ROT);
+        const int g = grid_for(ctx, cap / 2);
+        if (PAULI)
+            pauli_rot_kernel<(NW > 0 ? NW : 1), CPLX><<<g, kBlock, 0, ctx->stream>>>(cur.v, ctx->d_ctr, a);
+        else
+            majorana_rot_kernel<KW><<<g, kBlock, 0, ctx->stream>>>(cur.v, ctx->d_ctr, a);
+        ctx->prof.kernel_launches++;
+    }
+
+    void launch_trunc(const TruncArgs& t) {
+        PhaseScope ps(ctx, PH_TRUNC);
+        truncate_kernel<KW, CPLX, (PAULI ? NW : 0)><<<grid_for(ctx, cap / 2), kBlock, 0, ctx->stream>>>(
+            cur.v, ctx->d_ctr, t);
+        ctx->prof.kernel_launches++;
+    }
+
+    void launch_cliff(int begin, int end, u32 op) {
+        PhaseScope ps(ctx, PH_CLIFF);
+        clifford_kernel<(NW > 0 ? NW : 1), CPLX><<<grid_for(ctx, cap / 2), kBlock, 0, ctx->stream>>>(
+            cur.v, ctx->d_ctr, ctx->d_cliff + begin, end - begin, op);
+        ctx->prof.kernel_launches++;
+        reindex(cur, 0);
+    }
+
+    // top-k (src/pauli/truncate.h:21-38): keep the k largest |c|.  Ties at the
+    // cut are resolved by keeping the smallest keys (the reference keeps the
+    // ones that come first in its hash-map iteration order).
+    int topk(int k) {
+        int rc = sync_counters();
+        if (rc) return rc;
+        const u64 alive = ctx->h_ctr->alive;
+        if (k <= 0 || alive <= (u64)k) return FFG_OK;
+        // radix select of the (k+1)-th largest magnitude, 8 bits at a time
+        u64 prefix = 0, pmask = 0, rank = (u64)k;  // 0-based rank from the top
+        std::vector<u64> hist(256);
+        for (int shift = 56; shift >= 0; shift -= 8) {
+            CK(cudaMemsetAsync(ctx->d_hist, 0, 256 * 8, ctx->stream));
+            mag_hist_kernel<CPLX><<<grid_for(ctx, cap / 2), kBlock, 0, ctx->stream>>>(
+                cur.v, ctx->d_ctr, shift, prefix, pmask, ctx->d_hist);
+            CK(cudaMemcpyAsync(hist.data(), ctx->d_hist, 256 * 8, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            ctx->prof.kernel_launches++;
+            int b = 255;
+            for (; b >= 0; b--) {
+                if (rank < hist[b]) break;
+                rank -= hist[b];
+            }
+            if (b < 0) b = 0;
+            prefix |= (u64)b << shift;
+            pmask |= 255ull << shift;
+        }
+        const u64 cut = prefix;
+        // kill |c| < cut, gather ties
+        if (ctx->ties_cap < alive) {
+            if (ctx->d_ties) CK(cudaFree(ctx->d_ties));
+            ctx->ties_cap = std::max<size_t>(alive, 1024);
+            CK(cudaMalloc(&ctx->d_ties, (ctx->ties_cap + 1) * 8));
+        }
+        u64* d_nties = ctx->d_ties + ctx->ties_cap;
+        CK(cudaMemsetAsync(d_nties, 0, 8, ctx->stream));
+        topk_cut_kernel<CPLX><<<grid_for(ctx, cap / 2), kBlock, 0, ctx->stream>>>(
+            cur.v, ctx->d_ctr, cut, ctx->d_ties, d_nties, ctx->ties_cap);
+        ctx->prof.kernel_launches++;
+        u64 nties = 0;
+        CK(cudaMemcpyAsync(&nties, d_nties, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        rc = sync_counters();
+        if (rc) return rc;
+        const u64 now = ctx->h_ctr->alive;
+        if (now <= (u64)k) return FFG_OK;
+        u64 drop = now - (u64)k;
+        if (drop > nties) drop = nties;
+        // order ties by key, drop the largest keys
+        std::vector<u64> pos(nties);
+        CK(cudaMemcpy(pos.data(), ctx->d_ties, nties * 8, cudaMemcpyDeviceToHost));
+        std::vector<u64> keys((size_t)nties * KW);
+        for (u64 t = 0; t < nties; t++)
+            for (int w = 0; w < KW; w++)
+                CK(cudaMemcpy(&keys[t * KW + w], cur.v.key + (size_t)w * cap + pos[t], 8,
+                              cudaMemcpyDeviceToHost));
+        std::vector<u64> ord(nties);
+        for (u64 t = 0; t < nties; t++) ord[t] = t;
+        std::sort(ord.begin(), ord.end(), [&](u64 a, u64 b) {
+            // store planes are in the caller's lexicographic order
+            for (int w = 0; w < KW; w++)
+                if (keys[a * KW + w] != keys[b * KW + w]) return keys[a * KW + w] < keys[b * KW + w];
+            return false;
+        });
+        std::vector<u64> kill(drop);
+        for (u64 t = 0; t < drop; t++) kill[t] = pos[ord[nties - 1 - t]];
+        CK(cudaMemcpy(ctx->d_ties, kill.data(), drop * 8, cudaMemcpyHostToDevice));
+        kill_list_kernel<<<grid_for(ctx, drop), kBlock, 0, ctx->stream>>>(cur.v, ctx->d_ctr, ctx->d_ties, drop);
+        ctx->prof.kernel_launches++;
+        return sync_counters();
+    }
+
+    int run(const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
+            const std::vector<TruncArgs>& truncs) {
+        size_t i = 0;
+        while (i < ops.size()) {
+            size_t j = i;
+            int pending_topk = -1;
+            for (; j < ops.size() && j - i < (size_t)kChunkOps; j++) {
+                const Op& o = ops[j];
+                if (o.type == Op::ROT) {
+                    RotArgs a = rots[o.idx];
+                    a.op = (u32)j;
+                    launch_rot(a);
+                } else if (o.type == Op::TRUNC) {
+                    TruncArgs t = truncs[o.idx];
+                    t.op = (u32)j;
+                    if (t.thr || t.max_xweight >= 0) launch_trunc(t);
+                    if (o.topk > 0) {
+                        pending_topk = o.topk;
+                        j++;
+                        break;
+                    }
+                } else {
+                    launch_cliff(o.begin, o.end, (u32)j);
+                }
+            }
+            CK(cudaGetLastError());
+            int rc = sync_counters();
+            if (rc) return rc;
+            const DevCounters h = *ctx->h_ctr;
+            if (h.overflow) {
+                const size_t k = h.overflow - 1;
+                // grow: at least twice the entries the failed op could create
+                const u64 need = pow2_at_least(std::max<u64>(4 * h.n, 2 * cap));
+                DevCounters c = h;
+                c.overflow = 0;
+                *ctx->h_ctr = c;
+                CK(cudaMemcpyAsync(ctx->d_ctr, ctx->h_ctr, sizeof(DevCounters), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+                rc = compact_into(1 - active, need);
+                if (rc) return rc;
+                ctx->prof.regrows++;
+                // the other buffer is re-carved at the next compaction
+                i = k;
+                continue;
+            }
+            if (pending_topk > 0) {
+                rc = topk(pending_topk);
+                if (rc) return rc;
+            }
+            // compact when more than half of the positions are dead
+            const u64 dead = ctx->h_ctr->n - ctx->h_ctr->alive;
+            if (dead > 4096 && dead > ctx->h_ctr->alive) {
+                rc = compact_into(1 - active, cap);
+                if (rc) return rc;
+            }
+            i = j;
+        }
+        int rc = sync_counters();
+        if (rc) return rc;
+        if (ctx->h_ctr->n != ctx->h_ctr->alive) {
+            rc = compact_into(1 - active, cap);
+            if (rc) return rc;
+            rc = sync_counters();
+            if (rc) return rc;
+        }
+        return FFG_OK;
+    }
+
+    int extract(ffg_result** out, int kind, bool deterministic) {
+        const u64 n = ctx->h_ctr->n;
+        ffg_result* r = new ffg_result();
+        r->kind = kind;
+        r->nplanes = KW;
+        r->cplx = CPLX;
+        r->n = n;
+        r->ctx = ctx;
+        r->deterministic = deterministic;
+        r->device = ctx->device;
+        const size_t m = std::max<u64>(n, 1);
+        cudaError_t e = cudaMalloc(&r->key, (size_t)KW * m * 8);
+        if (e == cudaSuccess) e = cudaMalloc(&r->re, m * 8);
+        if (e == cudaSuccess && CPLX) e = cudaMalloc(&r->im, m * 8);
+        if (e == cudaSuccess) e = cudaMalloc(&r->dead, m);
+        if (e != cudaSuccess) {
+            ffg_result_free(r);
+            return set_err(ctx, FFG_ERR_CUDA, std::string("result allocation: ") + cudaGetErrorString(e));
+        }
+        for (int w = 0; w < KW; w++)
+            CK(cudaMemcpyAsync(r->key + (size_t)w * n, cur.v.key + (size_t)w * cap, n * 8,
+                               cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(r->re, cur.v.re, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+        if (CPLX) CK(cudaMemcpyAsync(r->im, cur.v.im, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemsetAsync(r->dead, 0, m, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        *out = r;
+        return FFG_OK;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// schedule construction
+// ---------------------------------------------------------------------------
+bool pauli_commute(const ffg_pauli_gate& a, const ffg_pauli_gate& b) {
+    int p = popc64(a.x[0] & b.z[0]) + popc64(a.x[1] & b.z[1]);
+    int q = popc64(a.z[0] & b.x[0]) + popc64(a.z[1] & b.x[1]);
+    return (p & 1) == (q & 1);
+}
+
+// Builds the op list; returns the batch sizes through `batches` when non-null.
+void build_pauli_ops(const ffg_pauli_gate* g, size_t ng, const ffg_pauli_params& p, int nw,
+                     std::vector<Op>& ops, std::vector<RotArgs>& rots, std::vector<TruncArgs>& truncs,
+                     std::vector<int64_t>* batches) {
+    int rot_count = 0;
+    auto add_rot = [&](size_t i) {
+        RotArgs a{};
+        const ffg_pauli_gate& G = g[i];
+        for (int w = 0; w < nw; w++) {
+            a.p[w] = G.x[w];
+            a.p[nw + w] = G.z[w];
+        }
+        a.c = std::cos(G.theta);
+        a.s = std::sin(G.theta);
+        a.maxdeg = p.maxdegree;
+        a.yP = popc64(G.x[0] & G.z[0]) + popc64(G.x[1] & G.z[1]);
+        rots.push_back(a);
+        ops.push_back({Op::ROT, (int)rots.size() - 1, 0, 0, 0});
+    };
+    auto add_trunc = [&](int rc) {
+        TruncArgs t{};
+        t.thr = p.mincoeff > 0;
+        t.tau = p.mincoeff;
+        t.max_xweight = (p.max_xweight >= 0 && p.xtrunc_period > 0 && (rc + 1) % p.xtrunc_period == 0)
+                            ? p.max_xweight
+                            : -1;
+        const int tk = p.topk > 0 ? p.topk : 0;
+        if (!t.thr && t.max_xweight < 0 && tk == 0) return;
+        truncs.push_back(t);
+        ops.push_back({Op::TRUNC, (int)truncs.size() - 1, 0, 0, tk});
+    };
+    auto add_cliff = [&](long long begin, long long end) {
+        ops.push_back({Op::CLIFF, 0, (int)begin, (int)end, 0});
+    };
+    long long cb = 0;
+    bool pending = false;
+    if (!p.batched) {
+        for (long long i = (long long)ng - 1; i >= 0; i--) {
+            if (g[i].kind != FFG_ROT) {
+                if (!pending) {
+                    cb = i;
+                    pending = true;
+                }
+            } else {
+                if (pending) {
+                    add_cliff(i + 1, cb + 1);
+                    pending = false;
+                }
+                add_rot((size_t)i);
+                if (batches) batches->push_back(1);
+                add_trunc(rot_count);
+                rot_count++;
+            }
+        }
+    } else {
+        std::vector<size_t> buf;
+        auto flush = [&]() {
+            size_t s = 0;
+            while (s < buf.size()) {
+                size_t e = s + 1;
+                while (e < buf.size()) {
+                    bool ok = true;
+                    for (size_t t = s; t < e && ok; t++)
+                        if (!pauli_commute(g[buf[e]], g[buf[t]])) ok = false;
+                    if (!ok) break;
+                    e++;
+                }
+                for (size_t t = s; t < e; t++) add_rot(buf[t]);
+                if (batches) batches->push_back((int64_t)(e - s));
+                rot_count += (int)(e - s);
+                add_trunc(rot_count - 1);
+                s = e;
+            }
+            buf.clear();
+        };
+        for (long long i = (long long)ng - 1; i >= 0; i--) {
+            if (g[i].kind != FFG_ROT) {
+                flush();
+                if (!pending) {
+                    cb = i;
+                    pending = true;
+                }
+            } else {
+                if (pending) {
+                    add_cliff(i + 1, cb + 1);
+                    pending = false;
+                }
+                buf.push_back((size_t)i);
+            }
+        }
+        flush();
+    }
+    if (pending) add_cliff(0, cb + 1);
+}
+
+// suffix-parity mask: bit t = parity of #{s in S : s > t}
+void suffix_parity(const uint64_t* alpha, u64* mg) {
+    int par = 0;
+    u64 out[4] = {0, 0, 0, 0};
+    for (int t = 255; t >= 0; t--) {
+        if (par) out[t >> 6] |= 1ull << (t & 63);
+        if ((alpha[t >> 6] >> (t & 63)) & 1ull) par ^= 1;
+    }
+    for (int w = 0; w < 4; w++) mg[w] = out[w];
+}
+
+template <int KW, bool CPLX, bool PAULI>
+int run_engine(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im, size_t n,
+               int on_device, const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
+               const std::vector<TruncArgs>& truncs, bool deterministic, ffg_result** out) {
+    Engine<KW, CPLX, PAULI> E(ctx);
+    int rc = E.load(keys, re, im, n, on_device, 0);
+    if (rc) return rc;
+    rc = E.run(ops, rots, truncs);
+    if (rc) return rc;
+    ctx->prof.apps = (int64_t)ctx->h_ctr->apps;
+    ctx->prof.emits = (int64_t)ctx->h_ctr->emits;
+    ctx->prof.peak_terms = (int64_t)ctx->h_ctr->peak;
+    ctx->prof.final_terms = (int64_t)ctx->h_ctr->n;
+    return E.extract(out, PAULI ? 1 : 2, deterministic);
+}
+
+void reset_profile(ffg_ctx* ctx) {
+    ctx->prof = ffg_profile{};
+}
+
+int upload_cliffords(ffg_ctx* ctx, const ffg_pauli_gate* g, size_t ng) {
+    if (ctx->cliff_cap < ng) {
+        if (ctx->d_cliff) CK(cudaFree(ctx->d_cliff));
+        ctx->cliff_cap = std::max<size_t>(ng, 256);
+        CK(cudaMalloc(&ctx->d_cliff, ctx->cliff_cap * sizeof(CliffordOp)));
+    }
+    std::vector<CliffordOp> h(ng);
+    for (size_t i = 0; i < ng; i++) h[i] = {g[i].kind, g[i].q0, g[i].q1, 0};
+    if (ng) CK(cudaMemcpyAsync(ctx->d_cliff, h.data(), ng * sizeof(CliffordOp), cudaMemcpyHostToDevice,
+                               ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FFG_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI (C linkage comes from the declarations in ffg.h)
+// ===========================================================================
+
+int ffg_create(ffg_ctx** out, int device) {
+    if (!out) return FFG_ERR_ARG;
+    *out = nullptr;
+    ffg_ctx* ctx = new ffg_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ctr, sizeof(DevCounters));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_ctr, sizeof(DevCounters));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_part, 2 * kMaxParts * sizeof(double) + 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_hist, 256 * 8);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "ffg_create: %s\n", cudaGetErrorString(e));
+        ffg_destroy(ctx);
+        return FFG_ERR_CUDA;
+    }
+    *out = ctx;
+    return FFG_OK;
+}
+
+int ffg_destroy(ffg_ctx* ctx) {
+    if (!ctx) return FFG_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto& b : ctx->buf)
+        if (b.p) cudaFree(b.p);
+    if (ctx->d_cliff) cudaFree(ctx->d_cliff);
+    if (ctx->d_part) cudaFree(ctx->d_part);
+    if (ctx->d_hist) cudaFree(ctx->d_hist);
+    if (ctx->d_ties) cudaFree(ctx->d_ties);
+    if (ctx->d_ctr) cudaFree(ctx->d_ctr);
+    if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
+    for (auto e : ctx->free_events) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return FFG_OK;
+}
+
+const char* ffg_last_error(const ffg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int ffg_set_profiling(ffg_ctx* ctx, int enabled) {
+    if (!ctx) return FFG_ERR_ARG;
+    ctx->profiling = enabled != 0;
+    return FFG_OK;
+}
+
+int ffg_profile_get(const ffg_ctx* ctx, ffg_profile* out) {
+    if (!ctx || !out) return FFG_ERR_ARG;
+    *out = ctx->prof;
+    return FFG_OK;
+}
+
+void* ffg_stream(const ffg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int ffg_pauli_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im,
+                        size_t n, const ffg_pauli_gate* gates, size_t ngates,
+                        const ffg_pauli_params* params, int on_device, ffg_result** out) {
+    if (!ctx || !out || !params || (n && (!keys || !re)) || (ngates && !gates)) return FFG_ERR_ARG;
+    *out = nullptr;
+    try {
+        auto t0 = std::chrono::steady_clock::now();
+        reset_profile(ctx);
+        CK(cudaSetDevice(ctx->device));
+        // validate gates; pick the key width
+        bool wide = false;
+        for (size_t i = 0; i < ngates; i++) {
+            const ffg_pauli_gate& G = gates[i];
+            if (G.kind < FFG_ROT || G.kind > FFG_CZ)
+                return set_err(ctx, FFG_ERR_ARG, "gate " + std::to_string(i) + ": unknown kind");
+            if (G.kind == FFG_ROT) {
+                if (G.x[1] || G.z[1]) wide = true;
+            } else {
+                const bool two = G.kind >= FFG_CNOT;
+                if (G.q0 < 0 || G.q0 >= 128 || (two && (G.q1 < 0 || G.q1 >= 128)))
+                    return set_err(ctx, FFG_ERR_ARG, "gate " + std::to_string(i) + ": qubit index out of range");
+                if (G.q0 >= 64 || (two && G.q1 >= 64)) wide = true;
+            }
+        }
+        bool cplx = false;
+        std::vector<uint64_t> hk;
+        if (!on_device) {
+            for (size_t i = 0; i < n && !wide; i++)
+                if (keys[n + i] || keys[3 * n + i]) wide = true;
+            if (im)
+                for (size_t i = 0; i < n && !cplx; i++)
+                    if (im[i] != 0.0) cplx = true;
+        } else {
+            // device input: inspect on the host (one copy of the key planes)
+            hk.resize(4 * n);
+            std::vector<double> him(n);
+            if (n) {
+                CK(cudaMemcpy(hk.data(), keys, 4 * n * 8, cudaMemcpyDeviceToHost));
+                if (im) CK(cudaMemcpy(him.data(), im, n * 8, cudaMemcpyDeviceToHost));
+            }
+            for (size_t i = 0; i < n && !wide; i++)
+                if (hk[n + i] || hk[3 * n + i]) wide = true;
+            if (im)
+                for (size_t i = 0; i < n && !cplx; i++)
+                    if (him[i] != 0.0) cplx = true;
+        }
+        const int nw = wide ? 2 : 1;
+        std::vector<Op> ops;
+        std::vector<RotArgs> rots;
+        std::vector<TruncArgs> truncs;
+        build_pauli_ops(gates, ngates, *params, nw, ops, rots, truncs, nullptr);
+        ctx->prof.n_gates = (int64_t)rots.size();
+        int rc = upload_cliffords(ctx, gates, ngates);
+        if (rc) return rc;
+        const bool det = params->deterministic != 0;
+        if (nw == 1 && !cplx)
+            rc = run_engine<2, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out);
+        else if (nw == 1)
+            rc = run_engine<2, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out);
+        else if (!cplx)
+            rc = run_engine<4, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out);
+        else
+            rc = run_engine<4, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out);
+        ctx->prof.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return rc;
+    } catch (const std::exception& ex) {
+        return set_err(ctx, FFG_ERR_STATE, ex.what());
+    }
+}
+
+int ffg_majorana_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im,
+                           size_t n, const ffg_majorana_gate* gates, size_t ngates,
+                           const ffg_majorana_params* params, int on_device, ffg_result** out) {
+    if (!ctx || !out || !params || (n && (!keys || !re)) || (ngates && !gates)) return FFG_ERR_ARG;
+    *out = nullptr;
+    try {
+        auto t0 = std::chrono::steady_clock::now();
+        reset_profile(ctx);
+        CK(cudaSetDevice(ctx->device));
+        int top = 0;  // highest plane used
+        auto plane_of = [](const uint64_t* a4) {
+            int t = 0;
+            for (int w = 0; w < 4; w++)
+                if (a4[w]) t = w;
+            return t;
+        };
+        for (size_t i = 0; i < ngates; i++) top = std::max(top, plane_of(gates[i].alpha));
+        std::vector<uint64_t> hk;
+        const uint64_t* kp = keys;
+        if (on_device && n) {
+            hk.resize(4 * n);
+            CK(cudaMemcpy(hk.data(), keys, 4 * n * 8, cudaMemcpyDeviceToHost));
+            kp = hk.data();
+        }
+        for (size_t i = 0; i < n; i++)
+            for (int w = 3; w > top; w--)
+                if (kp[(size_t)w * n + i]) top = w;
+        const int kw = top + 1;
+        std::vector<Op> ops;
+        std::vector<RotArgs> rots;
+        std::vector<TruncArgs> truncs;
+        TruncArgs t{};
+        t.thr = params->mincoeff > 0;
+        t.tau = params->mincoeff;
+        t.max_xweight = -1;
+        truncs.push_back(t);
+        for (long long i = (long long)ngates - 1; i >= 0; i--) {
+            const ffg_majorana_gate& G = gates[i];
+            RotArgs a{};
+            int deg = 0;
+            for (int w = 0; w < 4; w++) {
+                a.p[w] = G.alpha[w];
+                deg += popc64(G.alpha[w]);
+            }
+            suffix_parity(G.alpha, a.mg);
+            a.c = std::cos(G.theta);
+            a.s = std::sin(G.theta);
+            a.fr = G.r ? -a.s : 0.0;
+            a.fi = G.r ? 0.0 : a.s;
+            a.maxdeg = params->has_maxdegree ? params->maxdegree : 1 << 30;
+            a.gate_odd = deg & 1;
+            rots.push_back(a);
+            ops.push_back({Op::ROT, (int)rots.size() - 1, 0, 0, 0});
+            if (t.thr) ops.push_back({Op::TRUNC, 0, 0, 0, 0});
+        }
+        ctx->prof.n_gates = (int64_t)rots.size();
+        const bool det = params->deterministic != 0;
+        int rc;
+        switch (kw) {
+            case 1: rc = run_engine<1, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out); break;
+            case 2: rc = run_engine<2, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out); break;
+            case 3: rc = run_engine<3, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out); break;
+            default: rc = run_engine<4, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out); break;
+        }
+        ctx->prof.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return rc;
+    } catch (const std::exception& ex) {
+        return set_err(ctx, FFG_ERR_STATE, ex.what());
+    }
+}
+
+size_t ffg_result_size(const ffg_result* r) { return r ? r->n : 0; }
+int ffg_result_kind(const ffg_result* r) { return r ? r->kind : 0; }
+
+namespace {
+// host copy in caller layout ([4][n]) and, when deterministic, sorted order
+int result_to_host(const ffg_result* r, std::vector<uint64_t>& k4, std::vector<double>& re,
+                   std::vector<double>& im) {
+    ffg_ctx* ctx = r->ctx;
+    const size_t n = r->n;
+    k4.assign(4 * n, 0);
+    re.assign(n, 0.0);
+    im.assign(n, 0.0);
+    std::vector<uint64_t> planes((size_t)r->nplanes * n);
+    if (n) {
+        CK(cudaMemcpy(planes.data(), r->key, planes.size() * 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(re.data(), r->re, n * 8, cudaMemcpyDeviceToHost));
+        if (r->cplx) CK(cudaMemcpy(im.data(), r->im, n * 8, cudaMemcpyDeviceToHost));
+    }
+    for (int w = 0; w < r->nplanes; w++) {
+        int dst = w;
+        if (r->kind == 1) {
+            const int nw = r->nplanes / 2;
+            dst = (w < nw) ? w : 2 + (w - nw);
+        }
+        std::memcpy(&k4[(size_t)dst * n], &planes[(size_t)w * n], n * 8);
+    }
+    if (r->deterministic && n > 1) {
+        std::vector<size_t> ord(n);
+        for (size_t i = 0; i < n; i++) ord[i] = i;
+        std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
+            for (int w = 0; w < 4; w++)
+                if (k4[(size_t)w * n + a] != k4[(size_t)w * n + b]) return k4[(size_t)w * n + a] < k4[(size_t)w * n + b];
+            return false;
+        });
+        std::vector<uint64_t> k2(4 * n);
+        std::vector<double> r2(n), i2(n);
+        for (size_t t = 0; t < n; t++) {
+            for (int w = 0; w < 4; w++) k2[(size_t)w * n + t] = k4[(size_t)w * n + ord[t]];
+            r2[t] = re[ord[t]];
+            i2[t] = im[ord[t]];
+        }
+        k4.swap(k2);
+        re.swap(r2);
+        im.swap(i2);
+    }
+    return FFG_OK;
+}
+}  // namespace
+
+int ffg_result_copy(const ffg_result* r, uint64_t* keys, double* re, double* im) {
+    if (!r) return FFG_ERR_ARG;
+    ffg_ctx* ctx = r->ctx;
+    auto t0 = std::chrono::steady_clock::now();
+    cudaSetDevice(r->device);
+    const size_t n = r->n;
+    if (!r->deterministic) {
+        // direct plane copies into the caller's layout
+        if (n) {
+            for (int w = 0; w < r->nplanes; w++) {
+                int dst = w;
+                if (r->kind == 1) {
+                    const int nw = r->nplanes / 2;
+                    dst = (w < nw) ? w : 2 + (w - nw);
+                }
+                CK(cudaMemcpyAsync(keys + (size_t)dst * n, r->key + (size_t)w * n, n * 8,
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+            }
+            for (int w = 0; w < 4; w++) {
+                bool used = false;
+                for (int v = 0; v < r->nplanes; v++) {
+                    int dst = v;
+                    if (r->kind == 1) {
+                        const int nw = r->nplanes / 2;
+                        dst = (v < nw) ? v : 2 + (v - nw);
+                    }
+                    used = used || dst == w;
+                }
+                if (!used) std::memset(keys + (size_t)w * n, 0, n * 8);
+            }
+            CK(cudaMemcpyAsync(re, r->re, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+            if (im) {
+                if (r->cplx)
+                    CK(cudaMemcpyAsync(im, r->im, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+                else
+                    std::memset(im, 0, n * 8);
+            }
+            CK(cudaStreamSynchronize(ctx->stream));
+        }
+    } else {
+        std::vector<uint64_t> k4;
+        std::vector<double> hr, hi;
+        int rc = result_to_host(r, k4, hr, hi);
+        if (rc) return rc;
+        if (n) {
+            std::memcpy(keys, k4.data(), 4 * n * 8);
+            std::memcpy(re, hr.data(), n * 8);
+            if (im) std::memcpy(im, hi.data(), n * 8);
+        }
+    }
+    ctx->prof.seconds_d2h += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return FFG_OK;
+}
+
+int ffg_result_device(const ffg_result* r, const uint64_t** keys, size_t* stride, int* nplanes,
+                      const double** re, const double** im) {
+    if (!r) return FFG_ERR_ARG;
+    if (keys) *keys = (const uint64_t*)r->key;
+    if (stride) *stride = r->n;
+    if (nplanes) *nplanes = r->nplanes;
+    if (re) *re = r->re;
+    if (im) *im = r->cplx ? r->im : nullptr;
+    return FFG_OK;
+}
+
+namespace {
+template <int KW, bool CPLX>
+void launch_expect(const ffg_result* r, StoreView v, int mode, int nw, u64 b0, u64 b1, int parts) {
+    ffg_ctx* ctx = r->ctx;
+    expect_kernel<KW, CPLX><<<parts, kBlock, 0, ctx->stream>>>(v, r->n, mode, nw, b0, b1, ctx->d_part,
+                                                               ctx->d_part + kMaxParts);
+}
+
+int result_expect(const ffg_result* r, int mode, const uint64_t* b, double* ore, double* oim) {
+    if (!r || !ore || !oim) return FFG_ERR_ARG;
+    ffg_ctx* ctx = r->ctx;
+    cudaSetDevice(r->device);
+    const u64 b0 = b ? b[0] : 0, b1 = b ? b[1] : 0;
+    if (r->deterministic) {
+        std::vector<uint64_t> k4;
+        std::vector<double> hr, hi;
+        int rc = result_to_host(r, k4, hr, hi);
+        if (rc) return rc;
+        const size_t n = r->n;
+        double sr = 0.0, si = 0.0;
+        for (size_t i = 0; i < n; i++) {
+            double vr = 0.0, vi = 0.0;
+            bool use = false;
+            if (mode == 0) {
+                if (k4[i] == 0 && k4[n + i] == 0) {
+                    const int par = popc64(k4[2 * n + i] & b0) + popc64(k4[3 * n + i] & b1);
+                    const double sg = (par & 1) ? -1.0 : 1.0;
+                    vr = hr[i] * sg - hi[i] * 0.0;
+                    vi = hr[i] * 0.0 + hi[i] * sg;
+                    use = true;
+                }
+            } else {
+                bool paired = true;
+                u64 J[2] = {0, 0};
+                for (int w = 0; w < 4; w++) {
+                    const u64 x = k4[(size_t)w * n + i];
+                    const u64 ev = x & 0x5555555555555555ull, od = (x >> 1) & 0x5555555555555555ull;
+                    paired = paired && ev == od;
+                    u64 pj = 0;
+                    for (int t = 0; t < 32; t++) pj |= ((ev >> (2 * t)) & 1ull) << t;
+                    J[w >> 1] |= pj << (32 * (w & 1));
+                }
+                if (paired) {
+                    const int ex = popc64(J[0]) + popc64(J[1]) + 2 * (popc64(J[0] & b0) + popc64(J[1] & b1));
+                    double pr = 1.0, pi = 0.0;
+                    switch (ex & 3) {
+                        case 1: pr = 0.0; pi = 1.0; break;
+                        case 2: pr = -1.0; pi = 0.0; break;
+                        case 3: pr = 0.0; pi = -1.0; break;
+                        default: break;
+                    }
+                    vr = hr[i] * pr - hi[i] * pi;
+                    vi = hr[i] * pi + hi[i] * pr;
+                    use = true;
+                }
+            }
+            if (use) {
+                sr = sr + vr;
+                si = si + vi;
+            }
+        }
+        *ore = sr;
+        *oim = si;
+        return FFG_OK;
+    }
+    StoreView v{};
+    v.key = r->key;
+    v.re = r->re;
+    v.im = r->im;
+    v.dead = r->dead;
+    v.cap = r->n;
+    const int parts = (int)std::max<u64>(1, std::min<u64>((r->n + kBlock - 1) / kBlock, kMaxParts));
+    const int nw = r->kind == 1 ? r->nplanes / 2 : 0;
+    if (r->kind == 1) {
+        if (r->nplanes == 2 && !r->cplx) launch_expect<2, false>(r, v, mode, nw, b0, b1, parts);
+        else if (r->nplanes == 2) launch_expect<2, true>(r, v, mode, nw, b0, b1, parts);
+        else if (!r->cplx) launch_expect<4, false>(r, v, mode, nw, b0, b1, parts);
+        else launch_expect<4, true>(r, v, mode, nw, b0, b1, parts);
+    } else {
+        switch (r->nplanes) {
+            case 1: launch_expect<1, true>(r, v, mode, nw, b0, b1, parts); break;
+            case 2: launch_expect<2, true>(r, v, mode, nw, b0, b1, parts); break;
+            case 3: launch_expect<3, true>(r, v, mode, nw, b0, b1, parts); break;
+            default: launch_expect<4, true>(r, v, mode, nw, b0, b1, parts); break;
+        }
+    }
+    double* d_out = ctx->d_part + 2 * kMaxParts;
+    expect_final_kernel<<<1, 32, 0, ctx->stream>>>(ctx->d_part, ctx->d_part + kMaxParts, parts, d_out);
+    double h[2];
+    CK(cudaMemcpyAsync(h, d_out, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *ore = h[0];
+    *oim = h[1];
+    return FFG_OK;
+}
+}  // namespace
+
+int ffg_result_overlapwithzero(const ffg_result* r, double* re, double* im) {
+    if (!r || r->kind != 1) return FFG_ERR_ARG;
+    return result_expect(r, 0, nullptr, re, im);
+}
+
+int ffg_result_qubit_state(const ffg_result* r, const uint64_t* b, double* re, double* im) {
+    if (!r || r->kind != 1) return FFG_ERR_ARG;
+    return result_expect(r, 0, b, re, im);
+}
+
+int ffg_result_fock_state(const ffg_result* r, const uint64_t* b, double* re, double* im) {
+    if (!r || r->kind != 2) return FFG_ERR_ARG;
+    return result_expect(r, 1, b, re, im);
+}
+
+void ffg_result_free(ffg_result* r) {
+    if (!r) return;
+    cudaSetDevice(r->device);
+    if (r->key) cudaFree(r->key);
+    if (r->re) cudaFree(r->re);
+    if (r->im) cudaFree(r->im);
+    if (r->dead) cudaFree(r->dead);
+    delete r;
+}
+
+int ffg_abs_le(double re, double im, double tau) { return abs_le(re, im, tau) ? 1 : 0; }
+
+int64_t ffg_pauli_schedule(const ffg_pauli_gate* gates, size_t ngates, int batched, int64_t* sizes,
+                           int64_t cap) {
+    ffg_pauli_params p{};
+    p.maxdegree = 128;
+    p.batched = batched;
+    p.mincoeff = 1.0;  // force a truncation op after every batch
+    std::vector<Op> ops;
+    std::vector<RotArgs> rots;
+    std::vector<TruncArgs> truncs;
+    std::vector<int64_t> b;
+    build_pauli_ops(gates, ngates, p, 2, ops, rots, truncs, &b);
+    for (int64_t i = 0; i < (int64_t)b.size() && i < cap; i++) sizes[i] = b[i];
+    return (int64_t)b.size();
+}
+

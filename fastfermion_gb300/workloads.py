@@ -1,0 +1,91 @@
+"""Synthetic circuits for the propagation workloads (gate specifications only).
+
+Each generator returns a list of plain tuples so that the same circuit can be
+instantiated with this package's gate classes (``build_circuit``) or with any
+other implementation of the same gate types:
+
+* ``("ROT", paulis, qubits, theta)``   Pauli rotation exp(-i theta/2 P)
+* ``("H", q)``, ``("S", q)``, ``("CNOT", i, j)``, ``("SWAP", i, j)``, ``("CZ", i, j)``
+* ``("MROT", support, coeff, t)``      Majorana rotation exp(-i t/2 coeff*gamma_S)
+
+There is no dataset: every circuit is generated from its parameters and a seed.
+"""
+import math
+
+import numpy as np
+
+
+def chain_circuit(n=16, layers=10, seed=0, hi=math.pi / 8):
+    """16-qubit open chain: per layer RZZ(theta) on bonds (i, i+1), then RX(phi) on
+    every qubit; angles drawn in gate order from default_rng(seed).uniform(0, hi)."""
+    ngates = layers * ((n - 1) + n)
+    ang = np.random.default_rng(seed).uniform(0.0, hi, size=ngates)
+    out, a = [], 0
+    for _ in range(layers):
+        for i in range(n - 1):
+            out.append(("ROT", "ZZ", [i, i + 1], float(ang[a])))
+            a += 1
+        for i in range(n):
+            out.append(("ROT", "X", [i], float(ang[a])))
+            a += 1
+    return out
+
+
+def lattice_edges(lx=10, ly=10):
+    """Open lx-by-ly square lattice, site index 10*x + y style (ly*x + y): the
+    (x,y)-(x+1,y) edges first, then the (x,y)-(x,y+1) edges."""
+    edges = []
+    for x in range(lx - 1):
+        for y in range(ly):
+            edges.append((ly * x + y, ly * (x + 1) + y))
+    for x in range(lx):
+        for y in range(ly - 1):
+            edges.append((ly * x + y, ly * x + y + 1))
+    return edges
+
+
+def kicked_ising_circuit(theta_h, lx=10, ly=10, steps=20, theta_zz=-math.pi / 2):
+    """Kicked Ising: each step RZZ(theta_zz) on all lattice edges, then RX(theta_h)
+    on every site."""
+    edges = lattice_edges(lx, ly)
+    step = [("ROT", "ZZ", [i, j], theta_zz) for i, j in edges]
+    step += [("ROT", "X", [q], theta_h) for q in range(lx * ly)]
+    return step * steps
+
+
+KICKED_ISING_THETAS = (0.1, 0.3, 0.5, 0.7, 0.9, 1.1, math.pi / 2)
+
+
+def hubbard_step(lx=6, ly=6, t=1.0, u=4.0, dt=0.1):
+    """One Trotter step of the spinful 2D Fermi-Hubbard model in Majorana form.
+
+    Majorana index 4*site + 2*sigma + {0,1}, site = ly*x + y.  Hopping on the
+    horizontal bonds, then the vertical bonds (for each bond and spin the
+    normal-ordered strings of -0.5i*t*g_{4i+2s} g_{4j+2s+1} and
+    -0.5i*t*g_{4j+2s} g_{4i+2s+1}), then per site the non-identity terms of
+    0.25*U*(1 + i g0 g1)(1 + i g2 g3).  Every term becomes MROT(S, coeff, 2*dt).
+    """
+    def site(x, y):
+        return ly * x + y
+
+    horiz = [(site(x, y), site(x + 1, y)) for x in range(lx - 1) for y in range(ly)]
+    vert = [(site(x, y), site(x, y + 1)) for x in range(lx) for y in range(ly - 1)]
+    gates = []
+    for i, j in horiz + vert:
+        for s in (0, 1):
+            for a, b in ((4 * i + 2 * s, 4 * j + 2 * s + 1), (4 * j + 2 * s, 4 * i + 2 * s + 1)):
+                c = complex(0.0, -0.5 * t)
+                if a > b:  # g_a g_b = -g_b g_a
+                    a, b, c = b, a, -c
+                gates.append(("MROT", [a, b], c, 2 * dt))
+    if u != 0:
+        for s in range(lx * ly):
+            b0 = 4 * s
+            gates.append(("MROT", [b0, b0 + 1], complex(0.0, 0.25 * u), 2 * dt))
+            gates.append(("MROT", [b0 + 2, b0 + 3], complex(0.0, 0.25 * u), 2 * dt))
+            gates.append(("MROT", [b0, b0 + 1, b0 + 2, b0 + 3], complex(-0.25 * u, 0.0), 2 * dt))
+    return gates
+
+
+def hubbard_circuit(lx=6, ly=6, t=1.0, u=4.0, dt=0.1, steps=10):
+    return hubbard_step(lx, ly, t, u, dt) * steps

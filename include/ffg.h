@@ -1,0 +1,173 @@
+/*
+ * ffg.h -- C ABI of libffg, the GB300 (sm_103a) implementation of truncated
+ * Heisenberg-picture propagation of Pauli and Majorana polynomials.
+ *
+ * Plain C: integers, doubles and pointers only; every call returns FFG_OK (0)
+ * or a negative status, and ffg_last_error() gives the message.  One context
+ * owns one CUDA stream on one device and must not be used from two threads at
+ * once.  Device memory is pooled in the context and reused across calls.
+ *
+ * Key layout (all entry points): uint64 arrays of shape [4][n] (plane-major).
+ *   Pauli:    plane 0 = xory bits of qubits 0..63, plane 1 = xory of 64..127,
+ *             plane 2 = yorz bits of qubits 0..63, plane 3 = yorz of 64..127
+ *             (I=(0,0) X=(1,0) Y=(1,1) Z=(0,1), src/pauli/algebra.h:30-33)
+ *   Majorana: planes 0..3 = bits of Majorana indices 0..255
+ *             (src/majorana_algebra.h:30-33)
+ * Coefficients: separate re[n] and im[n] arrays of doubles (im may be NULL on
+ * input, meaning all-zero imaginary parts).  Input keys must be distinct.
+ *
+ * Reference interfaces replaced (paths relative to the fastfermion project):
+ *   ffg_pauli_propagate     pauli_gates::propagate, src/pauli/propagate.h:297-493,
+ *                           as bound in src/python_bind.cpp:392-425
+ *   ffg_majorana_propagate  majorana_gates::propagate, src/majorana_propagation.h:35-55,
+ *                           as bound in src/python_bind.cpp:490-527
+ *   ffg_result_overlapwithzero  PauliPolynomial::overlapwithzero, src/pauli/algebra.h:549-557
+ *   ffg_result_qubit_state  QubitProductState::operator(), src/qubitproductstate.h:73-88
+ *   ffg_result_fock_state   FockState::operator() on Majorana, src/fockstate.h:95-114
+ *   ffg_profile_get         prop_profile()/profile_get, src/pauli/propagate.h:34-65,
+ *                           src/python_bind.cpp:428-446
+ */
+#ifndef FFG_H_
+#define FFG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFG_OK 0
+#define FFG_ERR_ARG -1     /* invalid argument (bad gate, duplicate key, ...) */
+#define FFG_ERR_CUDA -2    /* CUDA runtime error (no device, out of memory, ...) */
+#define FFG_ERR_STATE -3   /* internal consistency check failed */
+
+/* gate kinds of the Pauli circuit table (src/pauli/gates.h:260-269) */
+#define FFG_ROT 0
+#define FFG_H 1
+#define FFG_S 2
+#define FFG_CNOT 3
+#define FFG_SWAP 4
+#define FFG_CZ 5
+
+typedef struct ffg_ctx ffg_ctx;
+typedef struct ffg_result ffg_result;
+
+/* One gate of a Pauli circuit, in circuit order (index 0 is applied to the
+ * state first, i.e. last in the Heisenberg picture). */
+typedef struct {
+    int32_t kind;    /* FFG_ROT, FFG_H, FFG_S, FFG_CNOT, FFG_SWAP, FFG_CZ */
+    int32_t q0, q1;  /* qubits of a Clifford gate (q1 unused for H and S) */
+    int32_t pad;
+    uint64_t x[2];   /* ROT axis: xory words */
+    uint64_t z[2];   /* ROT axis: yorz words */
+    double theta;    /* ROT: U = exp(-i theta/2 P) */
+} ffg_pauli_gate;
+
+/* One Majorana rotation U = exp(-i theta/2 * i^r gamma_S)
+ * (src/majorana_gates.h:17-60; theta already includes the monomial coefficient). */
+typedef struct {
+    uint64_t alpha[4];
+    double theta;
+    int32_t r;       /* 1 when gamma_S is not Hermitian (|S| mod 4 in {2,3}) */
+    int32_t pad;
+} ffg_majorana_gate;
+
+/* Truncation parameters; the defaults of the reference binding are
+ * maxdegree = 128, mincoeff = 0, topk = 0, max_xweight = -1,
+ * xtrunc_period = 1, batched = 1 (src/python_bind.cpp:413-416). */
+typedef struct {
+    int32_t maxdegree;      /* partner filter: emitted strings must have weight <= maxdegree */
+    int32_t topk;           /* > 0: keep the topk largest |c| after each truncation point */
+    double mincoeff;        /* > 0: erase |c| <= mincoeff */
+    int32_t max_xweight;    /* >= 0: erase X/Y weight > max_xweight every xtrunc_period rotations */
+    int32_t xtrunc_period;
+    int32_t batched;        /* 1: truncate once per maximal run of commuting rotations */
+    int32_t deterministic;  /* 1: expectation sums run in sorted-key order */
+} ffg_pauli_params;
+
+typedef struct {
+    int32_t has_maxdegree;  /* 0: no degree filter */
+    int32_t maxdegree;
+    double mincoeff;        /* > 0: erase |c| <= mincoeff after every gate */
+    int32_t deterministic;
+    int32_t pad;
+} ffg_majorana_params;
+
+/* Counters and per-phase device times of the most recent propagation. */
+typedef struct {
+    double seconds_total;     /* wall time of the call */
+    double seconds_rotations; /* device time in rotation kernels (profiling on) */
+    double seconds_truncate;  /* device time in truncation passes (profiling on) */
+    double seconds_clifford;  /* device time in Clifford segments + re-indexing */
+    double seconds_compact;   /* device time in compaction + re-indexing */
+    double seconds_h2d;       /* host-to-device input transfer */
+    double seconds_d2h;       /* device-to-host result transfer (ffg_result_copy) */
+    int64_t n_gates;          /* rotation gates applied */
+    int64_t apps;             /* sum over rotations of live terms entering the gate */
+    int64_t emits;            /* partners emitted that passed the degree filter */
+    int64_t peak_terms;       /* largest live-term count after any gate */
+    int64_t final_terms;
+    int64_t syncs;            /* host synchronisation points */
+    int64_t regrows;          /* capacity growths (each replays the pending gates) */
+    int64_t compactions;
+    int64_t kernel_launches;  /* kernels launched by the propagation */
+} ffg_profile;
+
+/* -------------------------------------------------------------------------- */
+int ffg_create(ffg_ctx** ctx, int device);
+int ffg_destroy(ffg_ctx* ctx);
+const char* ffg_last_error(const ffg_ctx* ctx);
+/* 1: record per-phase device times with CUDA events (adds synchronisation). */
+int ffg_set_profiling(ffg_ctx* ctx, int enabled);
+int ffg_profile_get(const ffg_ctx* ctx, ffg_profile* out);
+/* The context's CUDA stream (a cudaStream_t), for callers that time or order
+ * work around the library's launches. */
+void* ffg_stream(const ffg_ctx* ctx);
+
+/* Truncated Heisenberg propagation of a Pauli polynomial through a circuit.
+ * keys/re/im are host pointers when on_device == 0, device pointers of the
+ * context's device otherwise.  The result stays on the device until copied. */
+int ffg_pauli_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im,
+                        size_t n, const ffg_pauli_gate* gates, size_t ngates,
+                        const ffg_pauli_params* params, int on_device, ffg_result** out);
+
+/* Majorana propagation: gates applied last to first, threshold after every gate. */
+int ffg_majorana_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im,
+                           size_t n, const ffg_majorana_gate* gates, size_t ngates,
+                           const ffg_majorana_params* params, int on_device, ffg_result** out);
+
+/* -------------------------------------------------------------------------- */
+size_t ffg_result_size(const ffg_result* r);
+/* 1 for a Pauli result, 2 for a Majorana result */
+int ffg_result_kind(const ffg_result* r);
+/* Copies the terms to host arrays: keys [4][n], re[n], im[n] (im may be NULL).
+ * With the deterministic parameter set, terms come sorted lexicographically by
+ * (plane 0, plane 1, plane 2, plane 3); otherwise in store order. */
+int ffg_result_copy(const ffg_result* r, uint64_t* keys, double* re, double* im);
+/* Device pointers of the result (valid until ffg_result_free).  Key plane w of
+ * the n entries starts at keys + w * stride, w < *nplanes.  Pauli results use
+ * nplanes = 2*NW with the NW xory planes first (NW = 1 when every qubit index
+ * is below 64, else 2); Majorana results use one plane per 64 indices.  *im is
+ * NULL when the coefficients are real. */
+int ffg_result_device(const ffg_result* r, const uint64_t** keys, size_t* stride, int* nplanes,
+                      const double** re, const double** im);
+int ffg_result_overlapwithzero(const ffg_result* r, double* re, double* im);
+int ffg_result_qubit_state(const ffg_result* r, const uint64_t* b /* [2] */, double* re, double* im);
+int ffg_result_fock_state(const ffg_result* r, const uint64_t* b /* [2] */, double* re, double* im);
+void ffg_result_free(ffg_result* r);
+
+/* -------------------------------------------------------------------------- */
+/* Host-side helpers exposed for tests (no device work). */
+/* 1 when hypot(re, im) <= tau under round-to-nearest (the truncation rule). */
+int ffg_abs_le(double re, double im, double tau);
+/* Number of commuting batches the reference schedule forms for the rotations
+ * of a Pauli circuit (src/pauli/propagate.h:272-291 applied between Clifford
+ * segments); writes up to cap batch sizes in application order. */
+int64_t ffg_pauli_schedule(const ffg_pauli_gate* gates, size_t ngates, int batched, int64_t* sizes,
+                           int64_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,141 @@
+"""ctypes wrapper around the C oracle (oracle/ffo.c).
+
+TEST INFRASTRUCTURE ONLY: imported by the test-suite, by the smoke check and by
+the CPU-baseline leg of bench.py, never by the fastfermion_gb300 package.
+
+Gate tables use the numpy dtypes below; they have the same memory layout as the
+structs in oracle/ffo.h.  Keys are uint64 arrays of shape (4, n).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "libffo.so")
+
+PAULI_GATE = np.dtype([("kind", "<i4"), ("q0", "<i4"), ("q1", "<i4"), ("pad", "<i4"),
+                       ("x", "<u8", (2,)), ("z", "<u8", (2,)), ("theta", "<f8")])
+MAJORANA_GATE = np.dtype([("alpha", "<u8", (4,)), ("theta", "<f8"), ("r", "<i4"), ("pad", "<i4")])
+ROT, H, S, CNOT, SWAP, CZ = range(6)
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("maxdegree", ctypes.c_int32), ("topk", ctypes.c_int32),
+                ("mincoeff", ctypes.c_double), ("max_xweight", ctypes.c_int32),
+                ("xtrunc_period", ctypes.c_int32), ("batched", ctypes.c_int32),
+                ("n_threads", ctypes.c_int32)]
+
+
+def build(force=False):
+    """Compile libffo.so from ffo.c (gcc, OpenMP, no FMA contraction)."""
+    src = os.path.join(HERE, "ffo.c")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+        return LIB
+    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           src, "-o", LIB, "-lm"]
+    subprocess.run(cmd, check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        vp, i64, dp = ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)
+        L.ffo_pauli_propagate.restype = vp
+        L.ffo_pauli_propagate.argtypes = [vp, i64, vp, vp, vp, i64, ctypes.POINTER(_Params)]
+        L.ffo_majorana_propagate.restype = vp
+        L.ffo_majorana_propagate.argtypes = [vp, i64, vp, vp, vp, i64, ctypes.c_int32,
+                                             ctypes.c_int32, ctypes.c_double]
+        for f in ("ffo_size", "ffo_apps", "ffo_peak"):
+            getattr(L, f).restype = i64
+            getattr(L, f).argtypes = [vp]
+        L.ffo_copy.argtypes = [vp, vp, vp, vp]
+        L.ffo_free.argtypes = [vp]
+        L.ffo_overlapwithzero.argtypes = [vp, dp, dp]
+        L.ffo_qubit_state.argtypes = [vp, vp, dp, dp]
+        L.ffo_fock_state.argtypes = [vp, vp, dp, dp]
+        L.ffo_abs.restype = ctypes.c_double
+        L.ffo_abs.argtypes = [ctypes.c_double, ctypes.c_double]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size else None
+
+
+class OraclePoly:
+    """Result of an oracle propagation: keys (4, n), re, im in iteration order."""
+
+    def __init__(self, handle):
+        L = lib()
+        self.h = handle
+        n = L.ffo_size(handle)
+        self.keys = np.zeros((4, n), dtype=np.uint64)
+        self.re = np.zeros(n)
+        self.im = np.zeros(n)
+        if n:
+            L.ffo_copy(handle, _ptr(self.keys), _ptr(self.re), _ptr(self.im))
+        self.apps = L.ffo_apps(handle)
+        self.peak = L.ffo_peak(handle)
+
+    def __len__(self):
+        return self.re.size
+
+    def _pair(self, fn, *args):
+        r, i = ctypes.c_double(), ctypes.c_double()
+        fn(self.h, *args, ctypes.byref(r), ctypes.byref(i))
+        return complex(r.value, i.value)
+
+    def overlapwithzero(self):
+        return self._pair(lib().ffo_overlapwithzero)
+
+    def qubit_state(self, b0=0, b1=0):
+        b = np.array([b0, b1], dtype=np.uint64)
+        return self._pair(lib().ffo_qubit_state, _ptr(b))
+
+    def fock_state(self, b0=0, b1=0):
+        b = np.array([b0, b1], dtype=np.uint64)
+        return self._pair(lib().ffo_fock_state, _ptr(b))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ffo_free(self.h)
+            self.h = None
+
+
+def pauli_propagate(gates, keys, re, im=None, maxdegree=128, mincoeff=0.0, topk=0,
+                    max_xweight=-1, xtrunc_period=1, batched=True, n_threads=1):
+    gates = np.ascontiguousarray(gates, dtype=PAULI_GATE)
+    keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
+    re = np.ascontiguousarray(re, dtype=np.float64)
+    im = None if im is None else np.ascontiguousarray(im, dtype=np.float64)
+    p = _Params(int(maxdegree), int(topk), float(mincoeff), int(max_xweight),
+                int(xtrunc_period), int(bool(batched)), int(n_threads))
+    h = lib().ffo_pauli_propagate(_ptr(gates), gates.size, _ptr(keys), _ptr(re), _ptr(im),
+                                  re.size, ctypes.byref(p))
+    if not h:
+        raise ValueError("oracle rejected the circuit")
+    return OraclePoly(h)
+
+
+def majorana_propagate(gates, keys, re, im=None, maxdegree=None, mincoeff=0.0):
+    gates = np.ascontiguousarray(gates, dtype=MAJORANA_GATE)
+    keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
+    re = np.ascontiguousarray(re, dtype=np.float64)
+    im = None if im is None else np.ascontiguousarray(im, dtype=np.float64)
+    h = lib().ffo_majorana_propagate(_ptr(gates), gates.size, _ptr(keys), _ptr(re), _ptr(im),
+                                     re.size, int(maxdegree is not None),
+                                     int(maxdegree or 0), float(mincoeff))
+    return OraclePoly(h)
+
+
+def ffo_abs(re, im):
+    return lib().ffo_abs(float(re), float(im))
