@@ -92,11 +92,13 @@ __device__ __forceinline__ bool key_equals_cg(const StoreView& s, u64 i, const u
     return true;
 }
 
-// Returns the position of key k, or -1.  Entries are never removed from the
-// index (dead ones stay until compaction), so the probe chain of a key present
-// before the kernel started is never interrupted by an empty slot.
+// Returns the position of key k, or -1; *slot_at receives the index slot that
+// holds it.  Entries are never removed from the index (dead ones stay until
+// compaction), so the probe chain of a key present before the kernel started is
+// never interrupted by an empty slot.
 template <int KW>
-__device__ __forceinline__ long long lookup(const StoreView& s, const u64 (&k)[KW], u32* err) {
+__device__ __forceinline__ long long lookup(const StoreView& s, const u64 (&k)[KW], u32* err,
+                                            u64* slot_at = nullptr) {
     const u64 h = hash_key<KW>(k);
     const u32 fp = (u32)(h >> 32);
     u64 pos = h & s.hmask;
@@ -105,7 +107,10 @@ __device__ __forceinline__ long long lookup(const StoreView& s, const u64 (&k)[K
         if (e == kEmptySlot) return -1;
         if ((u32)(e >> 32) == fp) {
             const u32 idx = (u32)e;
-            if (key_equals_cg<KW>(s, idx, k)) return (long long)idx;
+            if (key_equals_cg<KW>(s, idx, k)) {
+                if (slot_at) *slot_at = pos;
+                return (long long)idx;
+            }
         }
         pos = (pos + 1) & s.hmask;
     }

@@ -110,25 +110,28 @@ __device__ __forceinline__ void store_coef(const StoreView& s, u64 i, cplx v) {
     if (CPLX) s.im[i] = v.im;
 }
 
-// Creates or revives the entry for key k with value v; returns the live-count
-// change.  j >= 0 names a dead entry holding k (revived in place); otherwise a
-// new position is appended after n_in and published in the index.
+// Creates the entry for key k with value v at a fresh position after n_in and
+// returns the live-count change.  When k is held by a dead entry (truncated
+// earlier, not yet compacted away; dead_slot names its index slot) the index
+// slot is re-pointed to the new position and the dead entry stays dead.  A
+// dead entry is never revived in place: its own thread in this kernel could
+// then see it live and process the pair a second time.
 template <int KW, bool CPLX>
 __device__ __forceinline__ int emit_partner(const StoreView& s, DevCounters* C, u64 n_in,
-                                            long long j, const u64 (&k)[KW], cplx v) {
+                                            long long dead_slot, const u64 (&k)[KW], cplx v) {
     const cplx nv = cadd({0.0, 0.0}, v);  // operator[] starts from complex zero
-    if (j >= 0) {
-        store_coef<CPLX>(s, (u64)j, nv);
-        s.dead[j] = 0;
-        return 1;
-    }
     const u64 pos = n_in + atomicAdd(&C->d_app, 1ull);
 #pragma unroll
     for (int w = 0; w < KW; w++) s.key[(u64)w * s.cap + pos] = k[w];
     store_coef<CPLX>(s, pos, nv);
     s.dead[pos] = 0;
     __threadfence();
-    insert<KW>(s, k, (u32)pos, &C->error, false);
+    if (dead_slot >= 0) {
+        const u64 e = __ldcg(&s.slots[dead_slot]);
+        atomicExch(&s.slots[dead_slot], (e & 0xffffffff00000000ull) | pos);
+    } else {
+        insert<KW>(s, k, (u32)pos, &C->error, false);
+    }
     return 1;
 }
 
@@ -173,7 +176,8 @@ __global__ void __launch_bounds__(kBlock) pauli_rot_kernel(StoreView s, DevCount
             // pauli_string_multiply(P, Q): src/pauli/algebra.h:227-233
             const int jQ = a.yP + yQ + 2 * zxQ - yK;
             const int jK = a.yP + yK + 2 * zxK - yQ;
-            const long long j = lookup<KW>(s, k, &C->error);
+            u64 js = 0;
+            const long long j = lookup<KW>(s, k, &C->error, &js);
             const cplx ci = load_coef<CPLX>(s, i);
             if (j >= 0 && !s.dead[j]) {
                 if ((u64)j < i) continue;  // the pair belongs to position j
@@ -187,7 +191,8 @@ __global__ void __launch_bounds__(kBlock) pauli_rot_kernel(StoreView s, DevCount
             } else {
                 store_coef<CPLX>(s, i, cscale(ci, a.c));
                 if (dK <= a.maxdeg) {
-                    d_alive += emit_partner<KW, CPLX>(s, C, n_in, j, k, cmul(cmul(ci, isin), ipow(jQ)));
+                    d_alive += emit_partner<KW, CPLX>(s, C, n_in, j >= 0 ? (long long)js : -1, k,
+                                                      cmul(cmul(ci, isin), ipow(jQ)));
                     emits++;
                 }
             }
@@ -235,7 +240,8 @@ __global__ void __launch_bounds__(kBlock) majorana_rot_kernel(StoreView s, DevCo
             // sign of gamma_S * gamma_Q: (-1)^merge_parity(Q, S) (src/bits_utils.h:14-38)
             const cplx sQ = {(mQ & 1) ? -1.0 : 1.0, 0.0};
             const cplx sK = {(mK & 1) ? -1.0 : 1.0, 0.0};
-            const long long j = lookup<KW>(s, k, &C->error);
+            u64 js = 0;
+            const long long j = lookup<KW>(s, k, &C->error, &js);
             const cplx ci = load_coef<true>(s, i);
             if (j >= 0 && !s.dead[j]) {
                 if ((u64)j < i) continue;
@@ -249,7 +255,8 @@ __global__ void __launch_bounds__(kBlock) majorana_rot_kernel(StoreView s, DevCo
             } else {
                 store_coef<true>(s, i, cscale(ci, a.c));
                 if (dK <= a.maxdeg) {
-                    d_alive += emit_partner<KW, true>(s, C, n_in, j, k, cmul(cmul(ci, F), sQ));
+                    d_alive += emit_partner<KW, true>(s, C, n_in, j >= 0 ? (long long)js : -1, k,
+                                                      cmul(cmul(ci, F), sQ));
                     emits++;
                 }
             }
@@ -394,11 +401,15 @@ __global__ void clear_slots_kernel(u64* slots, u64 nslots) {
     for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += stride) slots[i] = kEmptySlot;
 }
 
+// Rebuilds the index from the live entries only.  A dead entry may share its
+// key with a live one (a key truncated away and re-created later), so dead
+// entries must not be indexed.
 template <int KW>
 __global__ void __launch_bounds__(kBlock) index_kernel(StoreView s, DevCounters* C, int check_dup) {
     const u64 n = *(volatile u64*)&C->n;
     const u64 stride = (u64)gridDim.x * blockDim.x;
     for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (s.dead[i]) continue;
         u64 k[KW];
         load_key<KW>(s, i, k);
         insert<KW>(s, k, (u32)i, &C->error, check_dup != 0);
