@@ -50,7 +50,7 @@ EXPORTS = ["ffg_create", "ffg_destroy", "ffg_last_error", "ffg_set_profiling", "
            "ffg_pauli_propagate", "ffg_majorana_propagate", "ffg_result_size", "ffg_result_kind",
            "ffg_result_copy", "ffg_result_device", "ffg_result_overlapwithzero",
            "ffg_result_qubit_state", "ffg_result_fock_state", "ffg_result_free", "ffg_abs_le",
-           "ffg_pauli_schedule", "ffg_stream"]
+           "ffg_pauli_schedule", "ffg_stream", "ffg_pauli_rotations_noalloc"]
 
 
 def lib():
@@ -87,6 +87,9 @@ def lib():
             L.ffg_abs_le.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double]
             L.ffg_stream.restype = vp
             L.ffg_stream.argtypes = [vp]
+            L.ffg_pauli_rotations_noalloc.argtypes = [vp, vp, vp, vp, sz, vp, sz, ctypes.c_int32,
+                                                      vp, vp, vp, sz, ctypes.POINTER(sz),
+                                                      ctypes.c_char_p, sz]
             L.ffg_pauli_schedule.restype = i64
             L.ffg_pauli_schedule.argtypes = [vp, sz, ctypes.c_int, vp, i64]
             _lib = L

@@ -158,6 +158,37 @@ int ffg_result_fock_state(const ffg_result* r, const uint64_t* b /* [2] */, doub
 void ffg_result_free(ffg_result* r);
 
 /* -------------------------------------------------------------------------- */
+/* Allocation-free rotations.  No counterpart in the reference: this entry
+ * point exists for callers that cannot allocate device memory when they call
+ * it (code running under stream capture, where cudaMalloc/cudaFree are not
+ * permitted; loops that must not trigger the device-wide synchronisation of
+ * cudaFree; processes whose device memory is reserved by another allocator).
+ * It creates no context and calls no allocating CUDA or library routine: the
+ * term store lives in a fixed 65536-term device array inside libffg.
+ *
+ * Applies the FFG_ROT gates of gates[0..ngates) last to first, one reference
+ * conjugation each (partners of weight > maxdegree are not emitted), with no
+ * truncation, on the device polynomial keys_in [4][n] / re_in / im_in (im_in
+ * may be NULL), and writes the result to caller-allocated device arrays:
+ * key plane w at keys_out + w * out_cap, re_out[0..*n_out), im_out[0..*n_out).
+ * Work is issued on `stream` (a cudaStream_t; NULL = legacy default stream)
+ * and the call returns after it completes.
+ *   - n must be at most 32768 and the polynomial may not outgrow 65536 terms:
+ *     larger sizes return FFG_ERR_ARG with a message in errbuf (may be NULL);
+ *   - *n_out receives the result size even when out_cap is too small;
+ *   - the first call on a device looks up the device address of the array
+ *     (once per device, with that device current); make it before any stream
+ *     capture begins;
+ *   - all calls share the one array and each leaves its contents behind; calls
+ *     whose GPU work overlaps (e.g. on two streams) race and give wrong results.
+ */
+int ffg_pauli_rotations_noalloc(void* stream, const uint64_t* keys_in, const double* re_in,
+                                const double* im_in, size_t n, const ffg_pauli_gate* gates,
+                                size_t ngates, int32_t maxdegree, uint64_t* keys_out,
+                                double* re_out, double* im_out, size_t out_cap, size_t* n_out,
+                                char* errbuf, size_t errlen);
+
+/* -------------------------------------------------------------------------- */
 /* Host-side helpers exposed for tests (no device work). */
 /* 1 when hypot(re, im) <= tau under round-to-nearest (the truncation rule). */
 int ffg_abs_le(double re, double im, double tau);
