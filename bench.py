@@ -43,7 +43,15 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-roofline", action="store_true")
+    ap.add_argument("--thetas", default=None,
+                    help="comma-separated subset of theta_h (profiling runs; not a bench line)")
+    a = ap.parse_args()
+    if a.thetas:
+        global THETAS
+        THETAS = tuple(float(t) for t in a.thetas.split(","))
+    return a
 
 
 def tables():
@@ -282,9 +290,11 @@ def main():
     value = apps_all / t_max
 
     # roofline of the dominant kernel (rotation pass), per-launch CUDA events
-    a_p, e_p, _, rot_s, nrot = step_device(profiling=True)
-    alg_bytes = BYTES_PER_TERM * (2 * a_p + e_p)
-    achieved = alg_bytes / rot_s / 1e9 if rot_s > 0 else None
+    achieved = None
+    if not args.no_roofline:
+        a_p, e_p, _, rot_s, nrot = step_device(profiling=True)
+        alg_bytes = BYTES_PER_TERM * (2 * a_p + e_p)
+        achieved = alg_bytes / rot_s / 1e9 if rot_s > 0 else None
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk):
@@ -294,7 +304,7 @@ def main():
     # end-to-end through the public C ABI with host buffers
     ctx.set_profiling(False)
     e2e_times, h2d, d2h = [], 0, 0
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(0 if args.no_e2e else max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
         for tab in tabs:
             r = ctx.pauli_propagate(hk, hre, him, tab, dict(PARAMS))
@@ -304,8 +314,9 @@ def main():
             h2d += hk.nbytes + hre.nbytes + him.nbytes + tab.nbytes
             r.free()
         e2e_times.append(time.perf_counter() - t0)
-    n_e2e = len(e2e_times)
-    e2e_value = allsum(dist, apps_tot / args.steps * n_e2e) / allmax(dist, sum(e2e_times))
+    n_e2e = max(len(e2e_times), 1)
+    e2e_value = (allsum(dist, apps_tot / args.steps * n_e2e) / allmax(dist, sum(e2e_times))
+                 if e2e_times else None)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

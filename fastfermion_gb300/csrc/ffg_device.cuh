@@ -30,6 +30,7 @@ struct DevCounters {
     u64 peak;      // largest live count seen after a gate
     u64 emits;     // partners emitted that passed the degree filter
     u64 d_app;     // entries appended by the running kernel
+    u64 d_apps;    // fused passes: live terms created inside the pass that enter later gates
     long long d_alive;  // live-count change of the running kernel
     u32 done;      // blocks finished in the running kernel
     u32 overflow;  // 1 + op index that found the store too small (0 = none)

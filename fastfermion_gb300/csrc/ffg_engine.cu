@@ -22,12 +22,14 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "../../include/ffg.h"
 #include "ffg_kernels.cuh"
+#include "ffg_persist.cuh"
 
 using namespace ffg;
 
@@ -87,9 +89,12 @@ u64 pow2_at_least(u64 x) {
 
 int popc64(u64 x) { return __builtin_popcountll(x); }
 
+constexpr int kGroupD = 4;  // largest number of rotations fused in one pass (Pauli)
+typedef GroupArgs<kGroupD> GArgs;
+
 struct Op {
-    enum Type { ROT, TRUNC, CLIFF } type;
-    int idx;     // ROT: index into rot args; TRUNC: index into trunc args
+    enum Type { ROT, TRUNC, CLIFF, GROUP } type;
+    int idx;     // ROT: rot args; TRUNC: trunc args; GROUP: group args
     int begin;   // CLIFF: circuit range [begin, end)
     int end;
     int topk;    // TRUNC: top-k after threshold/x-weight
@@ -117,6 +122,20 @@ struct ffg_ctx {
     size_t ties_cap = 0;
     std::string err;
     bool profiling = false;
+    int group_d = 1;  // rotations fused per pass (1..4), FFG_GROUP_D overrides
+    bool persistent = true;  // one cooperative launch per run of ops (FFG_PERSISTENT=0 disables)
+    int persist_blocks_per_sm = 2;  // FFG_PERSIST_BPS overrides
+    PersistState* d_ps = nullptr;
+    DevOp* d_ops = nullptr;
+    size_t ops_cap = 0;
+    PairArgs* d_pairs = nullptr;
+    size_t pairs_cap = 0;
+    RotArgs* d_mrots = nullptr;
+    size_t mrots_cap = 0;
+    TruncArgs* d_truncs = nullptr;
+    size_t truncs_cap = 0;
+    GroupArgs<2>* d_groups2 = nullptr;
+    size_t groups2_cap = 0;
     ffg_profile prof{};
     std::vector<PendingEvent> events;
     std::vector<cudaEvent_t> free_events;
@@ -167,7 +186,7 @@ int ensure_buf(ffg_ctx* ctx, RawBuf& rb, size_t bytes) {
 
 int grid_for(const ffg_ctx* ctx, u64 items) {
     u64 b = (items + kBlock - 1) / kBlock;
-    u64 lim = (u64)ctx->num_sms * 4;
+    u64 lim = (u64)ctx->num_sms * 8;
     if (b < 1) b = 1;
     return (int)std::min(b, lim);
 }
@@ -413,8 +432,56 @@ struct Engine {
         return sync_counters();
     }
 
+    template <int D>
+    void launch_group_d(const GArgs& a) {
+        GroupArgs<D> b{};
+        for (int m = 0; m < (1 << D); m++)
+            for (int w = 0; w < 4; w++) b.psub[m][w] = a.psub[m][w];
+        for (int t = 0; t < D; t++) {
+            b.c[t] = a.c[t];
+            b.s[t] = a.s[t];
+            b.yP[t] = a.yP[t];
+        }
+        b.ng = a.ng;
+        b.maxdeg = a.maxdeg;
+        b.need = a.need;
+        b.op = a.op;
+        const int g = grid_for(ctx, cap / 2);
+        pauli_group_kernel<(NW > 0 ? NW : 1), CPLX, D><<<g, kBlock, 0, ctx->stream>>>(cur.v, ctx->d_ctr, b);
+    }
+
+    void launch_pair(const GArgs& a) {
+        PairArgs b{};
+        for (int w = 0; w < 4; w++) b.p[w] = a.psub[1][w];
+        b.c = a.c[0];
+        b.s = a.s[0];
+        b.yP = a.yP[0];
+        b.maxdeg = a.maxdeg;
+        b.need = a.need;
+        b.op = a.op;
+        const int g = grid_for(ctx, cap / 2);
+        pauli_pair_kernel<(NW > 0 ? NW : 1), CPLX><<<g, kBlock, 0, ctx->stream>>>(cur.v, ctx->d_ctr, b);
+    }
+
+    void launch_group(const GArgs& a) {
+        PhaseScope ps(ctx, PH_ROT);
+        if (!PAULI) return;
+        if (a.ng == 1) {
+            launch_pair(a);
+            ctx->prof.kernel_launches++;
+            return;
+        }
+        switch (ctx->group_d) {
+            case 1: launch_group_d<1>(a); break;
+            case 2: launch_group_d<2>(a); break;
+            case 3: launch_group_d<3>(a); break;
+            default: launch_group_d<4>(a); break;
+        }
+        ctx->prof.kernel_launches++;
+    }
+
     int run(const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
-            const std::vector<TruncArgs>& truncs) {
+            const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups) {
         size_t i = 0;
         while (i < ops.size()) {
             size_t j = i;
@@ -434,6 +501,10 @@ struct Engine {
                         j++;
                         break;
                     }
+                } else if (o.type == Op::GROUP) {
+                    GArgs a = groups[o.idx];
+                    a.op = (u32)j;
+                    launch_group(a);
                 } else {
                     launch_cliff(o.begin, o.end, (u32)j);
                 }
@@ -445,7 +516,7 @@ struct Engine {
             if (h.overflow) {
                 const size_t k = h.overflow - 1;
                 // grow: at least twice the entries the failed op could create
-                const u64 need = pow2_at_least(std::max<u64>(4 * h.n, 2 * cap));
+                const u64 need = pow2_at_least(std::max<u64>((u64)(2 << ctx->group_d) * h.n, 2 * cap));
                 DevCounters c = h;
                 c.overflow = 0;
                 *ctx->h_ctr = c;
@@ -479,6 +550,128 @@ struct Engine {
             if (rc) return rc;
         }
         return FFG_OK;
+    }
+
+    template <typename T>
+    int upload(T*& dptr, size_t& dcap, const std::vector<T>& h) {
+        if (dcap < h.size()) {
+            if (dptr) CK(cudaFree(dptr));
+            dcap = std::max<size_t>(h.size(), 64);
+            CK(cudaMalloc(&dptr, dcap * sizeof(T)));
+        }
+        if (!h.empty())
+            CK(cudaMemcpyAsync(dptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+        return FFG_OK;
+    }
+
+    // Runs the op list with the persistent kernel; the host only steps in to
+    // grow or compact the store.
+    int run_persistent(const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
+                       const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups) {
+        std::vector<DevOp> dops;
+        std::vector<PairArgs> pairs;
+        std::vector<GroupArgs<2>> g2;
+        dops.reserve(ops.size());
+        for (const Op& o : ops) {
+            if (o.type == Op::GROUP && groups[o.idx].ng == 2) {
+                const GArgs& a = groups[o.idx];
+                GroupArgs<2> b{};
+                for (int m = 0; m < 4; m++)
+                    for (int w = 0; w < 4; w++) b.psub[m][w] = a.psub[m][w];
+                for (int t = 0; t < 2; t++) {
+                    b.c[t] = a.c[t];
+                    b.s[t] = a.s[t];
+                    b.yP[t] = a.yP[t];
+                }
+                b.ng = 2;
+                b.maxdeg = a.maxdeg;
+                b.need = a.need;
+                g2.push_back(b);
+                dops.push_back({OP_GROUP2, (int)g2.size() - 1, 0, 0});
+            } else if (o.type == Op::GROUP) {
+                const GArgs& a = groups[o.idx];
+                PairArgs b{};
+                for (int w = 0; w < 4; w++) b.p[w] = a.psub[1][w];
+                b.c = a.c[0];
+                b.s = a.s[0];
+                b.yP = a.yP[0];
+                b.maxdeg = a.maxdeg;
+                b.need = a.need;
+                pairs.push_back(b);
+                dops.push_back({OP_PAIR, (int)pairs.size() - 1, 0, 0});
+            } else if (o.type == Op::ROT) {
+                dops.push_back({OP_MROT, o.idx, 0, 0});
+            } else if (o.type == Op::TRUNC) {
+                dops.push_back({OP_TRUNC, o.idx, 0, 0});
+            } else {
+                dops.push_back({OP_CLIFF, 0, o.begin, o.end});
+            }
+        }
+        int rc = upload(ctx->d_ops, ctx->ops_cap, dops);
+        if (!rc) rc = upload(ctx->d_pairs, ctx->pairs_cap, pairs);
+        if (!rc && !PAULI) rc = upload(ctx->d_mrots, ctx->mrots_cap, rots);
+        if (!rc) rc = upload(ctx->d_truncs, ctx->truncs_cap, truncs);
+        if (!rc) rc = upload(ctx->d_groups2, ctx->groups2_cap, g2);
+        if (rc) return rc;
+        auto kern = g2.empty() ? persistent_kernel<KW, CPLX, PAULI, false>
+                               : persistent_kernel<KW, CPLX, PAULI, PAULI>;
+        int per_sm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPBlock, 0));
+        if (per_sm < 1) return set_err(ctx, FFG_ERR_STATE, "persistent kernel does not fit on an SM");
+        const int grid = ctx->num_sms * std::min(per_sm, ctx->persist_blocks_per_sm);
+        size_t i = 0;
+        while (i < dops.size()) {
+            CK(cudaMemsetAsync(ctx->d_ps, 0, sizeof(PersistState), ctx->stream));
+            PersistArgs pa{};
+            pa.ops = ctx->d_ops;
+            pa.pairs = ctx->d_pairs;
+            pa.mrots = ctx->d_mrots;
+            pa.truncs = ctx->d_truncs;
+            pa.cliff = ctx->d_cliff;
+            pa.groups2 = ctx->d_groups2;
+            pa.op_begin = (int)i;
+            pa.op_end = (int)dops.size();
+            pa.compact_min = 4096;
+            StoreView v = cur.v;
+            DevCounters* C = ctx->d_ctr;
+            PersistState* ps = ctx->d_ps;
+            void* args[] = {(void*)&v, (void*)&C, (void*)&ps, (void*)&pa};
+            {
+                PhaseScope sc(ctx, PH_ROT);
+                CK(cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kPBlock), args, 0, ctx->stream));
+            }
+            ctx->prof.kernel_launches++;
+            PersistState h{};
+            CK(cudaMemcpyAsync(&h, ctx->d_ps, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+            rc = sync_counters();
+            if (rc) return rc;
+            if (h.stop_reason == 3) return set_err(ctx, FFG_ERR_STATE, "grid barrier timed out");
+            if (h.stop_reason == 4) return set_err(ctx, FFG_ERR_STATE, "persistent run entered with an error flag");
+            const DevCounters c = *ctx->h_ctr;
+            if (h.stop_reason == 1) {
+                const u64 need = pow2_at_least(std::max<u64>(8 * c.n, 2 * cap));
+                DevCounters z = c;
+                z.overflow = 0;
+                *ctx->h_ctr = z;
+                CK(cudaMemcpyAsync(ctx->d_ctr, ctx->h_ctr, sizeof(DevCounters), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+                rc = compact_into(1 - active, need);
+                if (rc) return rc;
+                ctx->prof.regrows++;
+            } else if (h.stop_reason == 2) {
+                rc = compact_into(1 - active, cap);
+                if (rc) return rc;
+            }
+            i = h.next_op;
+        }
+        int rc2 = sync_counters();
+        if (rc2) return rc2;
+        if (ctx->h_ctr->n != ctx->h_ctr->alive) {
+            rc2 = compact_into(1 - active, cap);
+            if (rc2) return rc2;
+            rc2 = sync_counters();
+        }
+        return rc2;
     }
 
     int extract(ffg_result** out, int kind, bool deterministic) {
@@ -522,9 +715,78 @@ bool pauli_commute(const ffg_pauli_gate& a, const ffg_pauli_gate& b) {
 }
 
 // Builds the op list; returns the batch sizes through `batches` when non-null.
+// GF(2) independence of the group's axes (x and z words as one 256-bit vector)
+struct Basis {
+    u64 v[kGroupD][4];
+    int piv[kGroupD];
+    int n = 0;
+    bool add(const u64* w4) {
+        u64 r[4] = {w4[0], w4[1], w4[2], w4[3]};
+        for (int b = 0; b < n; b++)
+            if ((r[piv[b] >> 6] >> (piv[b] & 63)) & 1ull)
+                for (int k = 0; k < 4; k++) r[k] ^= v[b][k];
+        int p = -1;
+        for (int k = 0; k < 4 && p < 0; k++)
+            if (r[k]) p = 64 * k + __builtin_ctzll(r[k]);
+        if (p < 0) return false;
+        for (int k = 0; k < 4; k++) v[n][k] = r[k];
+        piv[n++] = p;
+        return true;
+    }
+};
+
+// Splits a run of rotations (application order) into fused groups.
+void add_groups(const ffg_pauli_gate* g, const std::vector<size_t>& run, const ffg_pauli_params& p,
+                int nw, int dmax, std::vector<Op>& ops, std::vector<GArgs>& groups) {
+    size_t s = 0;
+    while (s < run.size()) {
+        Basis B;
+        size_t e = s;
+        while (e < run.size() && (int)(e - s) < dmax) {
+            const ffg_pauli_gate& G = g[run[e]];
+            const u64 w4[4] = {G.x[0], G.x[1], G.z[0], G.z[1]};
+            if (!B.add(w4)) break;
+            e++;
+        }
+        if (e == s) e = s + 1;  // an identity axis: a group of its own
+        GArgs a{};
+        a.ng = (int)(e - s);
+        a.maxdeg = p.maxdegree;
+        u64 axes[kGroupD][4] = {};
+        for (int t = 0; t < a.ng; t++) {
+            const ffg_pauli_gate& G = g[run[s + t]];
+            for (int w = 0; w < nw; w++) {
+                axes[t][w] = G.x[w];
+                axes[t][nw + w] = G.z[w];
+            }
+            a.c[t] = std::cos(G.theta);
+            a.s[t] = std::sin(G.theta);
+            a.yP[t] = popc64(G.x[0] & G.z[0]) + popc64(G.x[1] & G.z[1]);
+        }
+        for (int m = 0; m < (1 << kGroupD); m++)
+            for (int w = 0; w < 4; w++) {
+                u64 x = 0;
+                for (int t = 0; t < a.ng; t++)
+                    if ((m >> t) & 1) x ^= axes[t][w];
+                a.psub[m][w] = x;
+            }
+        u32 need = 0;
+        for (int t = 0; t < a.ng; t++)
+            for (int w = 0; w < nw; w++) {
+                if (axes[t][nw + w]) need |= 1u << w;          // z_P -> x_Q plane
+                if (axes[t][w]) need |= 1u << (nw + w);        // x_P -> z_Q plane
+            }
+        a.need = need;
+        groups.push_back(a);
+        ops.push_back({Op::GROUP, (int)groups.size() - 1, 0, 0, 0});
+        s = e;
+    }
+}
+
 void build_pauli_ops(const ffg_pauli_gate* g, size_t ng, const ffg_pauli_params& p, int nw,
                      std::vector<Op>& ops, std::vector<RotArgs>& rots, std::vector<TruncArgs>& truncs,
-                     std::vector<int64_t>* batches) {
+                     std::vector<int64_t>* batches, std::vector<GArgs>* groups = nullptr,
+                     int dmax = kGroupD) {
     int rot_count = 0;
     auto add_rot = [&](size_t i) {
         RotArgs a{};
@@ -569,7 +831,10 @@ void build_pauli_ops(const ffg_pauli_gate* g, size_t ng, const ffg_pauli_params&
                     add_cliff(i + 1, cb + 1);
                     pending = false;
                 }
-                add_rot((size_t)i);
+                if (groups)
+                    add_groups(g, std::vector<size_t>{(size_t)i}, p, nw, dmax, ops, *groups);
+                else
+                    add_rot((size_t)i);
                 if (batches) batches->push_back(1);
                 add_trunc(rot_count);
                 rot_count++;
@@ -588,7 +853,11 @@ void build_pauli_ops(const ffg_pauli_gate* g, size_t ng, const ffg_pauli_params&
                     if (!ok) break;
                     e++;
                 }
-                for (size_t t = s; t < e; t++) add_rot(buf[t]);
+                if (groups)
+                    add_groups(g, std::vector<size_t>(buf.begin() + s, buf.begin() + e), p, nw, dmax,
+                               ops, *groups);
+                else
+                    for (size_t t = s; t < e; t++) add_rot(buf[t]);
                 if (batches) batches->push_back((int64_t)(e - s));
                 rot_count += (int)(e - s);
                 add_trunc(rot_count - 1);
@@ -630,11 +899,17 @@ void suffix_parity(const uint64_t* alpha, u64* mg) {
 template <int KW, bool CPLX, bool PAULI>
 int run_engine(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im, size_t n,
                int on_device, const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
-               const std::vector<TruncArgs>& truncs, bool deterministic, ffg_result** out) {
+               const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups,
+               bool deterministic, ffg_result** out) {
     Engine<KW, CPLX, PAULI> E(ctx);
     int rc = E.load(keys, re, im, n, on_device, 0);
     if (rc) return rc;
-    rc = E.run(ops, rots, truncs);
+    bool has_topk = false;
+    for (const Op& o : ops) has_topk = has_topk || (o.type == Op::TRUNC && o.topk > 0);
+    if (ctx->persistent && ctx->group_d <= 2 && !has_topk)
+        rc = E.run_persistent(ops, rots, truncs, groups);
+    else
+        rc = E.run(ops, rots, truncs, groups);
     if (rc) return rc;
     ctx->prof.apps = (int64_t)ctx->h_ctr->apps;
     ctx->prof.emits = (int64_t)ctx->h_ctr->emits;
@@ -672,6 +947,12 @@ int ffg_create(ffg_ctx** out, int device) {
     *out = nullptr;
     ffg_ctx* ctx = new ffg_ctx();
     ctx->device = device;
+    if (const char* d = getenv("FFG_GROUP_D")) {
+        const int v = atoi(d);
+        if (v >= 1 && v <= kGroupD) ctx->group_d = v;
+    }
+    if (const char* d = getenv("FFG_PERSISTENT")) ctx->persistent = atoi(d) != 0;
+    if (const char* d = getenv("FFG_PERSIST_BPS")) ctx->persist_blocks_per_sm = std::max(1, atoi(d));
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -679,6 +960,7 @@ int ffg_create(ffg_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_ctr, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_part, 2 * kMaxParts * sizeof(double) + 2 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_hist, 256 * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ps, sizeof(PersistState));
     if (e != cudaSuccess) {
         fprintf(stderr, "ffg_create: %s\n", cudaGetErrorString(e));
         ffg_destroy(ctx);
@@ -698,6 +980,12 @@ int ffg_destroy(ffg_ctx* ctx) {
     if (ctx->d_part) cudaFree(ctx->d_part);
     if (ctx->d_hist) cudaFree(ctx->d_hist);
     if (ctx->d_ties) cudaFree(ctx->d_ties);
+    if (ctx->d_ps) cudaFree(ctx->d_ps);
+    if (ctx->d_ops) cudaFree(ctx->d_ops);
+    if (ctx->d_pairs) cudaFree(ctx->d_pairs);
+    if (ctx->d_mrots) cudaFree(ctx->d_mrots);
+    if (ctx->d_truncs) cudaFree(ctx->d_truncs);
+    if (ctx->d_groups2) cudaFree(ctx->d_groups2);
     if (ctx->d_ctr) cudaFree(ctx->d_ctr);
     if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
     for (auto e : ctx->free_events) cudaEventDestroy(e);
@@ -772,19 +1060,22 @@ int ffg_pauli_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, co
         std::vector<Op> ops;
         std::vector<RotArgs> rots;
         std::vector<TruncArgs> truncs;
-        build_pauli_ops(gates, ngates, *params, nw, ops, rots, truncs, nullptr);
-        ctx->prof.n_gates = (int64_t)rots.size();
+        std::vector<GArgs> groups;
+        build_pauli_ops(gates, ngates, *params, nw, ops, rots, truncs, nullptr, &groups, ctx->group_d);
+        int64_t nrot = 0;
+        for (const auto& gr : groups) nrot += gr.ng;
+        ctx->prof.n_gates = nrot;
         int rc = upload_cliffords(ctx, gates, ngates);
         if (rc) return rc;
         const bool det = params->deterministic != 0;
         if (nw == 1 && !cplx)
-            rc = run_engine<2, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out);
+            rc = run_engine<2, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out);
         else if (nw == 1)
-            rc = run_engine<2, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out);
+            rc = run_engine<2, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out);
         else if (!cplx)
-            rc = run_engine<4, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out);
+            rc = run_engine<4, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out);
         else
-            rc = run_engine<4, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out);
+            rc = run_engine<4, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out);
         ctx->prof.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return rc;
     } catch (const std::exception& ex) {
@@ -851,10 +1142,10 @@ int ffg_majorana_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re,
         const bool det = params->deterministic != 0;
         int rc;
         switch (kw) {
-            case 1: rc = run_engine<1, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out); break;
-            case 2: rc = run_engine<2, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out); break;
-            case 3: rc = run_engine<3, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out); break;
-            default: rc = run_engine<4, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, det, out); break;
+            case 1: rc = run_engine<1, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out); break;
+            case 2: rc = run_engine<2, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out); break;
+            case 3: rc = run_engine<3, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out); break;
+            default: rc = run_engine<4, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out); break;
         }
         ctx->prof.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return rc;

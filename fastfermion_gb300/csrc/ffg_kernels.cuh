@@ -671,3 +671,395 @@ __global__ void kill_list_kernel(StoreView s, DevCounters* C, const u64* list, u
 }
 
 }  // namespace ffg
+
+namespace ffg {
+
+// ---------------------------------------------------------------------------
+// Fused pass over a group of up to D consecutive rotations of one commuting
+// batch whose axes are linearly independent (as GF(2) vectors).
+//
+// For a term Q let A = {t : Q anticommutes with P_t}.  Because the axes commute,
+// every member of the orbit M_S = Q * prod_{t in S} P_t (S subset of A) has the
+// same A, the members are distinct (independent axes), and the gates of the
+// group only ever pair members of the same orbit.  Applying the group gate by
+// gate is therefore, orbit by orbit, a sequence of butterflies over the
+// hypercube of subsets of A, taken in gate order: stage t pairs M_S with
+// M_{S+t}.  The present member with the lowest store position owns the orbit,
+// gathers the present members, runs the stages in registers with the
+// reference's exact per-gate arithmetic, degree filter and creation rule, and
+// writes the members back (new ones are appended and indexed).
+// ---------------------------------------------------------------------------
+template <int D>
+struct GroupArgs {
+    u64 psub[1 << D][4];  // XOR of the axes of each gate subset (planes in store order)
+    double c[D], s[D];
+    int yP[D];
+    int ng;               // gates in the group (1..D)
+    int maxdeg;
+    u32 need;             // bit w: key plane w takes part in the anticommutation test
+    u32 op;
+};
+
+template <int NW>
+__device__ __forceinline__ int popc_planes(const u64 (&k)[2 * NW], int lo) {
+    int r = 0;
+#pragma unroll
+    for (int w = 0; w < NW; w++) r += __popcll(k[lo + w]);
+    return r;
+}
+
+// Processes the orbit of the live term at position i (anticommutation pattern
+// A) when i owns it.  Adds to the thread's live-count, emitted-partner and
+// in-pass application counters.
+template <int NW, bool CPLX, int D>
+__device__ __forceinline__ void group_orbit(const StoreView& s, DevCounters* C, const GroupArgs<D>& a,
+                                            u64 n_in, u64 i, u32 A, long long& d_alive,
+                                            long long& emits, long long& extra_apps,
+                                            u64* app_ctr = nullptr) {
+    constexpr int KW = 2 * NW;
+    constexpr int M = 1 << D;
+    u64 q[KW];
+    load_key<KW>(s, i, q);
+    // look up every member of the orbit; loc[m] = store position of a present
+    // member, or the index slot of a dead one
+    u32 loc[M];
+    u32 present = 1u, wasdead = 0u;
+    loc[0] = (u32)i;
+    bool owner = true;
+#pragma unroll
+    for (int m = 1; m < M; m++) {
+        loc[m] = 0u;
+        if ((m & ~A) != 0) continue;
+        u64 k[KW];
+#pragma unroll
+        for (int w = 0; w < KW; w++) k[w] = q[w] ^ a.psub[m][w];
+        u64 sl = 0;
+        const long long j = lookup<KW>(s, k, &C->error, &sl);
+        if (j >= 0) {
+            if (!s.dead[j]) {
+                present |= 1u << m;
+                loc[m] = (u32)j;
+                if ((u64)j < i) owner = false;
+            } else {
+                wasdead |= 1u << m;
+                loc[m] = (u32)sl;
+            }
+        }
+    }
+    if (!owner) return;
+    cplx c[M];
+#pragma unroll
+    for (int m = 0; m < M; m++) {
+        c[m] = {0.0, 0.0};
+        if ((present >> m) & 1u) c[m] = load_coef<CPLX>(s, loc[m]);
+    }
+    const u32 present0 = present;
+    // stages in gate order
+#pragma unroll
+    for (int t = 0; t < D; t++) {
+        if (t >= a.ng || !((A >> t) & 1u)) continue;
+        const u64* P = a.psub[1 << t];
+        const cplx isin = {0.0, a.s[t]};
+        int created = 0;
+#pragma unroll
+        for (int u = 0; u < M; u++) {
+            if ((u & ~A) != 0 || ((u >> t) & 1)) continue;
+            const int v = u | (1 << t);
+            const bool pu = (present >> u) & 1u, pv = (present >> v) & 1u;
+            if (!pu && !pv) continue;
+            // degrees, Y counts and phases of P_t * member
+            // (pauli_string_multiply, src/pauli/algebra.h:227-233)
+            int du = 0, dv = 0, yu = 0, yv = 0, zxu = 0, zxv = 0;
+#pragma unroll
+            for (int w = 0; w < NW; w++) {
+                const u64 xu = q[w] ^ a.psub[u][w], zu = q[NW + w] ^ a.psub[u][NW + w];
+                const u64 xv = q[w] ^ a.psub[v][w], zv = q[NW + w] ^ a.psub[v][NW + w];
+                du += __popcll(xu | zu);
+                dv += __popcll(xv | zv);
+                yu += __popcll(xu & zu);
+                yv += __popcll(xv & zv);
+                zxu += __popcll(P[NW + w] & xu);
+                zxv += __popcll(P[NW + w] & xv);
+            }
+            const int ju = a.yP[t] + yu + 2 * zxu - yv;  // P_t * M_u -> M_v
+            const int jv = a.yP[t] + yv + 2 * zxv - yu;  // P_t * M_v -> M_u
+            const bool to_u = pv && du <= a.maxdeg;
+            const bool to_v = pu && dv <= a.maxdeg;
+            cplx nu = c[u], nv = c[v];
+            if (pu) nu = cscale(c[u], a.c[t]);
+            if (pv) nv = cscale(c[v], a.c[t]);
+            if (to_u) nu = cadd(pu ? nu : cplx{0.0, 0.0}, cmul(cmul(c[v], isin), ipow(jv)));
+            if (to_v) nv = cadd(pv ? nv : cplx{0.0, 0.0}, cmul(cmul(c[u], isin), ipow(ju)));
+            emits += (int)to_u + (int)to_v;
+            if (!pu && to_u) {
+                present |= 1u << u;
+                created++;
+            }
+            if (!pv && to_v) {
+                present |= 1u << v;
+                created++;
+            }
+            c[u] = nu;
+            c[v] = nv;
+        }
+        extra_apps += (long long)created * (a.ng - 1 - t);
+    }
+    // write back
+#pragma unroll
+    for (int m = 0; m < M; m++) {
+        if (!((present >> m) & 1u)) continue;
+        if ((present0 >> m) & 1u) {
+            store_coef<CPLX>(s, loc[m], c[m]);
+            continue;
+        }
+        u64 k[KW];
+#pragma unroll
+        for (int w = 0; w < KW; w++) k[w] = q[w] ^ a.psub[m][w];
+        const u64 pos = n_in + atomicAdd(app_ctr ? app_ctr : &C->d_app, 1ull);
+#pragma unroll
+        for (int w = 0; w < KW; w++) s.key[(u64)w * s.cap + pos] = k[w];
+        store_coef<CPLX>(s, pos, c[m]);
+        s.dead[pos] = 0;
+        __threadfence();
+        if ((wasdead >> m) & 1u) {
+            const u64 ent = __ldcg(&s.slots[loc[m]]);
+            atomicExch(&s.slots[loc[m]], (ent & 0xffffffff00000000ull) | pos);
+        } else {
+            insert<KW>(s, k, (u32)pos, &C->error, false);
+        }
+        d_alive += 1;
+    }
+}
+
+constexpr int kScanR = 8;                     // terms tested per thread per tile
+constexpr int kTile = kBlock * kScanR;
+
+// One pass of a rotation group over the store.  Each block walks tiles of
+// kTile positions: every thread first issues the loads of its kScanR terms
+// together (the planes the axes touch plus the dead flags) and queues the
+// anticommuting live ones in shared memory; then the block works through the
+// queue, one orbit per thread.
+template <int NW, bool CPLX, int D>
+__global__ void __launch_bounds__(kBlock) pauli_group_kernel(StoreView s, DevCounters* C,
+                                                             GroupArgs<D> a) {
+    constexpr int KW = 2 * NW;
+    __shared__ Entry e;
+    __shared__ long long sh[kBlock / 32];
+    __shared__ u32 queue[kTile];
+    __shared__ u32 qn;
+    if (threadIdx.x == 0) {
+        volatile DevCounters* V = C;
+        const u64 n = V->n;
+        int skip = V->overflow != 0 || V->error != 0;
+        // an orbit of 2^ng members may be created from each present term
+        if (!skip && (n << a.ng) > s.cap) {
+            atomicCAS(&C->overflow, 0u, a.op + 1u);
+            skip = 1;
+        }
+        e.n = n;
+        e.alive = V->alive;
+        e.skip = skip;
+    }
+    __syncthreads();
+    long long d_alive = 0, emits = 0, extra_apps = 0;
+    if (!e.skip) {
+        const u64 n_in = e.n;
+        const u64 ntiles = (n_in + kTile - 1) / kTile;
+        for (u64 tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            if (threadIdx.x == 0) qn = 0;
+            __syncthreads();
+            const u64 base = tile * kTile;
+            u64 pl[kScanR][KW];
+            unsigned char dd[kScanR];
+#pragma unroll
+            for (int r = 0; r < kScanR; r++) {
+                const u64 i = base + (u64)r * kBlock + threadIdx.x;
+                const bool in = i < n_in;
+#pragma unroll
+                for (int w = 0; w < KW; w++)
+                    pl[r][w] = (in && ((a.need >> w) & 1u)) ? s.key[(u64)w * s.cap + i] : 0ull;
+                dd[r] = in ? s.dead[i] : 1;
+            }
+#pragma unroll
+            for (int r = 0; r < kScanR; r++) {
+                u32 A = 0;
+#pragma unroll
+                for (int t = 0; t < D; t++) {
+                    if (t >= a.ng) break;
+                    const u64* P = a.psub[1 << t];
+                    u64 par = 0;
+#pragma unroll
+                    for (int w = 0; w < NW; w++) par ^= (pl[r][w] & P[NW + w]) ^ (pl[r][NW + w] & P[w]);
+                    A |= (u32)(__popcll(par) & 1) << t;
+                }
+                const bool act = A != 0 && !dd[r];
+                const u32 vote = __ballot_sync(0xffffffffu, act);
+                if (vote) {
+                    const int lane = threadIdx.x & 31;
+                    u32 slot0 = 0;
+                    if (lane == 0) slot0 = atomicAdd(&qn, (u32)__popc(vote));
+                    slot0 = __shfl_sync(0xffffffffu, slot0, 0);
+                    if (act) queue[slot0 + __popc(vote & ((1u << lane) - 1u))] =
+                        ((u32)(r * kBlock + threadIdx.x) << 4) | A;
+                }
+            }
+            __syncthreads();
+            const u32 nq = qn;
+            for (u32 k = threadIdx.x; k < nq; k += blockDim.x) {
+                const u32 ent = queue[k];
+                group_orbit<NW, CPLX, D>(s, C, a, n_in, base + (ent >> 4), ent & 15u, d_alive, emits,
+                                         extra_apps);
+            }
+            __syncthreads();
+        }
+    }
+    // fold counters; apps = sum over the group's gates of the live terms entering it
+    const long long tot = block_sum_ll(d_alive, sh);
+    const long long em = block_sum_ll(emits, sh);
+    const long long xa = block_sum_ll(extra_apps, sh);
+    if (threadIdx.x == 0) {
+        if (tot) atomicAdd((u64*)&C->d_alive, (u64)tot);
+        if (em) atomicAdd(&C->emits, (u64)em);
+        if (xa) atomicAdd(&C->d_apps, (u64)xa);
+        __threadfence();
+        const u32 prev = atomicAdd(&C->done, 1u);
+        if (prev == gridDim.x - 1) {
+            __threadfence();
+            volatile DevCounters* V = C;
+            const u64 app = V->d_app;
+            const long long da = V->d_alive;
+            V->n = e.n + app;
+            const u64 al = (u64)((long long)e.alive + da);
+            V->alive = al;
+            if (!e.skip) {
+                V->apps = V->apps + (u64)a.ng * e.alive + V->d_apps;
+                if (al > V->peak) V->peak = al;
+            }
+            V->d_app = 0;
+            V->d_alive = 0;
+            V->d_apps = 0;
+            V->done = 0;
+            __threadfence();
+        }
+    }
+}
+
+}  // namespace ffg
+
+namespace ffg {
+
+// ---------------------------------------------------------------------------
+// Lean single-rotation pass (the pair butterfly of pauli_rot_kernel) tuned for
+// memory-level parallelism: few registers so that many terms are in flight,
+// and the dependent loads of a pair grouped into as few round trips as
+// possible:
+//   1. the planes the axis touches + the dead flag of position i
+//   2. (anticommuting, live) the remaining planes + the coefficient of i
+//   3. the index probe for the partner key
+//   4. the partner's key words, dead flag and coefficient, issued together
+// ---------------------------------------------------------------------------
+struct PairArgs {
+    u64 p[4];        // axis planes in store order (x words, then z words)
+    double c, s;
+    int yP;
+    int maxdeg;
+    u32 need;        // planes that take part in the anticommutation test
+    u32 op;
+};
+
+template <int NW, bool CPLX>
+__global__ void __launch_bounds__(kBlock, 5) pauli_pair_kernel(StoreView s, DevCounters* C, PairArgs a) {
+    constexpr int KW = 2 * NW;
+    __shared__ Entry e;
+    __shared__ long long sh[kBlock / 32];
+    kernel_enter(C, s.cap, true, a.op, &e);
+    long long d_alive = 0, emits = 0;
+    if (!e.skip) {
+        const u64 n_in = e.n;
+        const u64 stride = (u64)gridDim.x * blockDim.x;
+        for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += stride) {
+            u64 q[KW];
+#pragma unroll
+            for (int w = 0; w < KW; w++) q[w] = ((a.need >> w) & 1u) ? s.key[(u64)w * s.cap + i] : 0ull;
+            const unsigned char di = s.dead[i];
+            u64 par = 0;
+#pragma unroll
+            for (int w = 0; w < NW; w++) par ^= (q[w] & a.p[NW + w]) ^ (q[NW + w] & a.p[w]);
+            if (!(__popcll(par) & 1) || di) continue;
+#pragma unroll
+            for (int w = 0; w < KW; w++)
+                if (!((a.need >> w) & 1u)) q[w] = s.key[(u64)w * s.cap + i];
+            const cplx ci = load_coef<CPLX>(s, i);
+            // partner key K = P*Q, its degree and the two phases
+            int yQ = 0, yK = 0, zxQ = 0, zxK = 0, dQ = 0, dK = 0;
+#pragma unroll
+            for (int w = 0; w < NW; w++) {
+                const u64 xk = q[w] ^ a.p[w], zk = q[NW + w] ^ a.p[NW + w];
+                yQ += __popcll(q[w] & q[NW + w]);
+                yK += __popcll(xk & zk);
+                zxQ += __popcll(a.p[NW + w] & q[w]);
+                zxK += __popcll(a.p[NW + w] & xk);
+                dQ += __popcll(q[w] | q[NW + w]);
+                dK += __popcll(xk | zk);
+            }
+            const int jQ = a.yP + yQ + 2 * zxQ - yK;  // P*Q -> K
+            const int jK = a.yP + yK + 2 * zxK - yQ;  // P*K -> Q
+            // probe for K; at a fingerprint match fetch key, dead flag and
+            // coefficient of the candidate in one round trip
+            u64 k[KW];
+#pragma unroll
+            for (int w = 0; w < KW; w++) k[w] = q[w] ^ a.p[w];
+            const u64 h = hash_key<KW>(k);
+            const u32 fp = (u32)(h >> 32);
+            u64 pos = h & s.hmask;
+            long long j = -1;
+            u64 jslot = 0;
+            bool jdead = false;
+            cplx cj = {0.0, 0.0};
+            for (u64 probe = 0; probe <= s.hmask; probe++) {
+                const u64 ent = __ldcg(&s.slots[pos]);
+                if (ent == kEmptySlot) break;
+                if ((u32)(ent >> 32) == fp) {
+                    const u32 idx = (u32)ent;
+                    bool eq = true;
+                    u64 kk[KW];
+#pragma unroll
+                    for (int w = 0; w < KW; w++) kk[w] = __ldcg(&s.key[(u64)w * s.cap + idx]);
+                    const unsigned char dj = s.dead[idx];
+                    const cplx cc = {s.re[idx], CPLX ? s.im[idx] : 0.0};
+#pragma unroll
+                    for (int w = 0; w < KW; w++) eq = eq && kk[w] == k[w];
+                    if (eq) {
+                        j = idx;
+                        jslot = pos;
+                        jdead = dj != 0;
+                        cj = cc;
+                        break;
+                    }
+                }
+                pos = (pos + 1) & s.hmask;
+                if (probe == s.hmask) atomicOr(&C->error, 2u);
+            }
+            const cplx isin = {0.0, a.s};
+            if (j >= 0 && !jdead) {
+                if ((u64)j < i) continue;  // the pair belongs to position j
+                cplx ni = cscale(ci, a.c), nj = cscale(cj, a.c);
+                if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
+                if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
+                emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
+                store_coef<CPLX>(s, i, ni);
+                store_coef<CPLX>(s, (u64)j, nj);
+            } else {
+                store_coef<CPLX>(s, i, cscale(ci, a.c));
+                if (dK <= a.maxdeg) {
+                    d_alive += emit_partner<KW, CPLX>(s, C, n_in, j >= 0 ? (long long)jslot : -1, k,
+                                                      cmul(cmul(ci, isin), ipow(jQ)));
+                    emits++;
+                }
+            }
+        }
+    }
+    kernel_exit(C, e, d_alive, sh, true, emits);
+}
+
+}  // namespace ffg
