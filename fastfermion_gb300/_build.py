@@ -30,7 +30,8 @@ def build(force=False, verbose=False):
     """Compile libffg.so unless it is up to date; returns its path."""
     if not force and not _stale():
         return LIB
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false",
+    extra = os.environ.get("FFG_BUILD_FLAGS", "").split()
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", *extra,
            "-Xcompiler", "-fPIC,-ffp-contract=off", "-shared",
            "-I", os.path.join(os.path.dirname(HERE), "include"),
            *[os.path.join(CSRC, s) for s in SOURCES], "-o", LIB + ".tmp"]

@@ -37,7 +37,7 @@ class Profile(ctypes.Structure):
         "seconds_compact", "seconds_h2d", "seconds_d2h")] + [
         (n, ctypes.c_int64) for n in (
             "n_gates", "apps", "emits", "peak_terms", "final_terms", "syncs", "regrows", "compactions",
-            "kernel_launches")]
+            "kernel_launches", "orbit_batches", "orbit_fallbacks", "orbit_groups", "orbit_max_group")]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -30,6 +30,7 @@
 #include "../../include/ffg.h"
 #include "ffg_kernels.cuh"
 #include "ffg_persist.cuh"
+#include "ffg_orbit.cuh"
 
 using namespace ffg;
 
@@ -100,6 +101,13 @@ struct Op {
     int topk;    // TRUNC: top-k after threshold/x-weight
 };
 
+// One commuting run of rotations and the truncation that follows it.
+struct BatchInfo {
+    int first;   // op index of the first rotation
+    int nrot;    // rotation ops (consecutive)
+    int trunc;   // op index of the trailing truncation, or -1
+};
+
 struct PendingEvent {
     cudaEvent_t a, b;
     int phase;
@@ -136,6 +144,15 @@ struct ffg_ctx {
     size_t truncs_cap = 0;
     GroupArgs<2>* d_groups2 = nullptr;
     size_t groups2_cap = 0;
+    bool orbit = true;          // batch-orbit path for long commuting runs (FFG_ORBIT=0 disables)
+    int orbit_min_gates = 4;    // shortest run sent to the batch-orbit path
+    BatchGate* d_bgates = nullptr;
+    size_t bgates_cap = 0;
+    char* d_oscratch = nullptr;
+    size_t oscratch_bytes = 0;
+    OrbitCounters* d_oc = nullptr;
+    OrbitCounters* h_oc = nullptr;  // pinned
+    RawBuf bigpool;                 // global-memory tables of large orbit groups
     ffg_profile prof{};
     std::vector<PendingEvent> events;
     std::vector<cudaEvent_t> free_events;
@@ -169,6 +186,20 @@ constexpr int kChunkOps = 128;
         }                                                                                 \
     } while (0)
 
+#ifdef FFG_ORBIT_CHECK
+#define OSTEP(name)                                              \
+    do {                                                         \
+        cudaError_t e_ = cudaGetLastError();                     \
+        if (e_ == cudaSuccess) e_ = cudaStreamSynchronize(ctx->stream); \
+        if (e_ != cudaSuccess) {                                 \
+            ctx->err = std::string(name) + ": " + cudaGetErrorString(e_); \
+            return FFG_ERR_CUDA;                                 \
+        }                                                        \
+    } while (0)
+#else
+#define OSTEP(name) CK(cudaGetLastError())
+#endif
+
 int set_err(ffg_ctx* ctx, int code, const std::string& m) {
     ctx->err = m;
     return code;
@@ -176,10 +207,26 @@ int set_err(ffg_ctx* ctx, int code, const std::string& m) {
 
 int ensure_buf(ffg_ctx* ctx, RawBuf& rb, size_t bytes) {
     if (rb.bytes >= bytes) return FFG_OK;
-    if (rb.p) CK(cudaFree(rb.p));
+    if (rb.p) {
+        const cudaError_t e = cudaFree(rb.p);
+        if (e != cudaSuccess) {
+            char m[256];
+            snprintf(m, sizeof m, "cudaFree of a %zu-byte buffer at %p (growing to %zu bytes): %s", rb.bytes,
+                     (void*)rb.p, bytes, cudaGetErrorString(e));
+            ctx->err = m;
+            return FFG_ERR_CUDA;
+        }
+    }
     rb.p = nullptr;
     rb.bytes = 0;
-    CK(cudaMalloc(&rb.p, bytes));
+    const cudaError_t e = cudaMalloc(&rb.p, bytes);
+    if (e != cudaSuccess) {
+        char m[256];
+        snprintf(m, sizeof m, "cudaMalloc of %zu bytes: %s", bytes, cudaGetErrorString(e));
+        ctx->err = m;
+        rb.p = nullptr;
+        return FFG_ERR_CUDA;
+    }
     rb.bytes = bytes;
     return FFG_OK;
 }
@@ -291,6 +338,7 @@ struct Engine {
         cap = newcap;
         active = to;
         reindex(cur, 0);
+        index_valid = true;
         ctx->prof.compactions++;
         CK(cudaGetLastError());
         return FFG_OK;
@@ -564,13 +612,19 @@ struct Engine {
         return FFG_OK;
     }
 
-    // Runs the op list with the persistent kernel; the host only steps in to
-    // grow or compact the store.
-    int run_persistent(const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
-                       const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups) {
-        std::vector<DevOp> dops;
+    // ---------------------------------------------------------------------
+    // persistent runs
+    // ---------------------------------------------------------------------
+    std::vector<DevOp> dops;
+    void (*pkern)(StoreView, DevCounters*, PersistState*, PersistArgs) = nullptr;
+    int pgrid = 0;
+    bool index_valid = true;  // the index describes the live entries of cur
+
+    int prepare_persistent(const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
+                           const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups) {
         std::vector<PairArgs> pairs;
         std::vector<GroupArgs<2>> g2;
+        dops.clear();
         dops.reserve(ops.size());
         for (const Op& o : ops) {
             if (o.type == Op::GROUP && groups[o.idx].ng == 2) {
@@ -613,14 +667,26 @@ struct Engine {
         if (!rc) rc = upload(ctx->d_truncs, ctx->truncs_cap, truncs);
         if (!rc) rc = upload(ctx->d_groups2, ctx->groups2_cap, g2);
         if (rc) return rc;
-        auto kern = g2.empty() ? persistent_kernel<KW, CPLX, PAULI, false>
-                               : persistent_kernel<KW, CPLX, PAULI, PAULI>;
+        pkern = g2.empty() ? persistent_kernel<KW, CPLX, PAULI, false> : persistent_kernel<KW, CPLX, PAULI, PAULI>;
         int per_sm = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPBlock, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pkern, kPBlock, 0));
         if (per_sm < 1) return set_err(ctx, FFG_ERR_STATE, "persistent kernel does not fit on an SM");
-        const int grid = ctx->num_sms * std::min(per_sm, ctx->persist_blocks_per_sm);
-        size_t i = 0;
-        while (i < dops.size()) {
+        pgrid = ctx->num_sms * std::min(per_sm, ctx->persist_blocks_per_sm);
+        return FFG_OK;
+    }
+
+    void launch_reindex() {
+        reindex(cur, 0);
+        index_valid = true;
+    }
+
+    // Runs ops [begin, end) with the persistent kernel; the host only steps in
+    // to grow or compact the store.
+    int exec_persistent(size_t begin, size_t end) {
+        if (!index_valid) launch_reindex();
+        size_t i = begin;
+        int rc = FFG_OK;
+        while (i < end) {
             CK(cudaMemsetAsync(ctx->d_ps, 0, sizeof(PersistState), ctx->stream));
             PersistArgs pa{};
             pa.ops = ctx->d_ops;
@@ -630,7 +696,7 @@ struct Engine {
             pa.cliff = ctx->d_cliff;
             pa.groups2 = ctx->d_groups2;
             pa.op_begin = (int)i;
-            pa.op_end = (int)dops.size();
+            pa.op_end = (int)end;
             pa.compact_min = 4096;
             StoreView v = cur.v;
             DevCounters* C = ctx->d_ctr;
@@ -638,7 +704,7 @@ struct Engine {
             void* args[] = {(void*)&v, (void*)&C, (void*)&ps, (void*)&pa};
             {
                 PhaseScope sc(ctx, PH_ROT);
-                CK(cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kPBlock), args, 0, ctx->stream));
+                CK(cudaLaunchCooperativeKernel((void*)pkern, dim3(pgrid), dim3(kPBlock), args, 0, ctx->stream));
             }
             ctx->prof.kernel_launches++;
             PersistState h{};
@@ -646,7 +712,6 @@ struct Engine {
             rc = sync_counters();
             if (rc) return rc;
             if (h.stop_reason == 3) return set_err(ctx, FFG_ERR_STATE, "grid barrier timed out");
-            if (h.stop_reason == 4) return set_err(ctx, FFG_ERR_STATE, "persistent run entered with an error flag");
             const DevCounters c = *ctx->h_ctr;
             if (h.stop_reason == 1) {
                 const u64 need = pow2_at_least(std::max<u64>(8 * c.n, 2 * cap));
@@ -664,14 +729,279 @@ struct Engine {
             }
             i = h.next_op;
         }
-        int rc2 = sync_counters();
-        if (rc2) return rc2;
+        return rc;
+    }
+
+    int finish() {
+        int rc = sync_counters();
+        if (rc) return rc;
         if (ctx->h_ctr->n != ctx->h_ctr->alive) {
-            rc2 = compact_into(1 - active, cap);
-            if (rc2) return rc2;
-            rc2 = sync_counters();
+            rc = compact_into(1 - active, cap);
+            if (rc) return rc;
+            rc = sync_counters();
         }
-        return rc2;
+        return rc;
+    }
+
+    int run_persistent(const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
+                       const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups) {
+        int rc = prepare_persistent(ops, rots, truncs, groups);
+        if (!rc) rc = exec_persistent(0, dops.size());
+        if (!rc) rc = finish();
+        return rc;
+    }
+
+    // ---------------------------------------------------------------------
+    // batch-orbit runs (Pauli, batched mode)
+    // ---------------------------------------------------------------------
+    u32* retry_list = nullptr;
+    u32* nretry = nullptr;
+
+    // Block-level pass over the groups in `list`; returns 0 when every group
+    // fit, 2 when the output store overflowed, else a negative status.
+    int exec_big_groups(const StoreView& out, OrbitScratch& sc, const OrbitBatchArgs& a, u32 nbig) {
+        constexpr int NWo = PAULI ? NW : 1;
+        u32* list = sc.big;
+        u32* other = retry_list;
+        u64 rcap = 1ull << 16;
+        while (nbig > 0) {
+            const u32 grid = std::min<u32>(nbig, (u32)ctx->num_sms);
+            const u64 region = align256((size_t)KW * rcap * 8 + rcap * 8 * (CPLX ? 2 : 1) + 2 * rcap * 4 + 8);
+            int rc = ensure_buf(ctx, ctx->bigpool, region * grid);
+            if (rc) return rc;
+            BigPool bp{};
+            bp.base = ctx->bigpool.p;
+            bp.region_bytes = region;
+            bp.rcap = (u32)rcap;
+            bp.retry = other;
+            bp.nretry = nretry;
+            CK(cudaMemsetAsync(nretry, 0, 4, ctx->stream));
+            {
+                PhaseScope ps(ctx, PH_ROT);
+                orbit_process_big<NWo, CPLX><<<grid, 1024, 0, ctx->stream>>>(cur.v, out, sc, ctx->d_oc, a, bp,
+                                                                             list, nbig);
+                OSTEP("orbit_process_big");
+                ctx->prof.kernel_launches++;
+            }
+            CK(cudaGetLastError());
+            u32 hr = 0;
+            CK(cudaMemcpyAsync(ctx->h_oc, ctx->d_oc, sizeof(OrbitCounters), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(&hr, nretry, 4, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            ctx->prof.syncs++;
+            if (ctx->h_oc->chk_code)
+                return set_err(ctx, FFG_ERR_STATE, "orbit self-check " + std::to_string(ctx->h_oc->chk_code) + " a=" +
+                                                       std::to_string(ctx->h_oc->chk_a) + " b=" + std::to_string(ctx->h_oc->chk_b) +
+                                                       " c=" + std::to_string(ctx->h_oc->chk_c));
+            if (ctx->h_oc->overflow & 1u) return 2;
+            if (hr == 0) return 0;
+            std::swap(list, other);
+            nbig = hr;
+            rcap *= 4;
+            if (rcap > (1ull << 26)) return set_err(ctx, FFG_ERR_STATE, "orbit group larger than 2^26 terms");
+        }
+        return 0;
+    }
+
+    OrbitScratch carve_scratch(u64 cap_in) {
+        OrbitScratch sc{};
+        u64 hc = pow2_at_least(std::max<u64>(2 * cap_in, 1024));
+        size_t need = align256((size_t)kAW * cap_in * 8) + align256((size_t)KW * cap_in * 8) +
+                      8 * align256(cap_in * 4) + align256(hc * 8) + 256;
+        if (ctx->oscratch_bytes < need) {
+            if (ctx->d_oscratch && cudaFree(ctx->d_oscratch) != cudaSuccess) return sc;
+            ctx->d_oscratch = nullptr;
+            ctx->oscratch_bytes = 0;
+            if (cudaMalloc(&ctx->d_oscratch, need) != cudaSuccess) return sc;
+            ctx->oscratch_bytes = need;
+        }
+        char* p = ctx->d_oscratch;
+        sc.amask = (u64*)p;
+        p += align256((size_t)kAW * cap_in * 8);
+        sc.gkey = (u64*)p;
+        p += align256((size_t)KW * cap_in * 8);
+        sc.rep = (u32*)p;
+        p += align256(cap_in * 4);
+        sc.cnt = (u32*)p;
+        p += align256(cap_in * 4);
+        sc.off = (u32*)p;
+        p += align256(cap_in * 4);
+        sc.fill = (u32*)p;
+        p += align256(cap_in * 4);
+        sc.order = (u32*)p;
+        p += align256(cap_in * 4);
+        sc.groups = (u32*)p;
+        p += align256(cap_in * 4);
+        sc.big = (u32*)p;
+        p += align256(cap_in * 4);
+        retry_list = (u32*)p;
+        p += align256(cap_in * 4);
+        nretry = (u32*)p;
+        p += 256;
+        sc.gslots = (u64*)p;
+        sc.gmask = hc - 1;
+        sc.cap_in = cap_in;
+        return sc;
+    }
+
+    // Applies rotations [g0, g0+k) of the batch gate table and the batch-end
+    // truncation t (may be null) to the store.  Returns 1 when a group
+    // outgrew the shared-memory table (nothing was changed), else a status.
+    int exec_orbit_batch(int g0, int k, const TruncArgs* t, int maxdeg) {
+        const u64 n_in = ctx->h_ctr->n;  // dense store: no dead entries
+        if (n_in == 0) return FFG_OK;
+        const u64 cap_in = std::max<u64>(n_in, 1024);
+        OrbitScratch sc = carve_scratch(cap_in);
+        if (!sc.amask) return set_err(ctx, FFG_ERR_CUDA, "orbit scratch allocation failed");
+        OrbitBatchArgs a{};
+        a.gates = ctx->d_bgates + g0;
+        a.k = k;
+        a.maxdeg = maxdeg;
+        a.thr = t ? t->thr : 0;
+        a.tau = t ? t->tau : 0.0;
+        a.max_xweight = t ? t->max_xweight : -1;
+        u64 out_cap = std::max<u64>(cap, pow2_at_least(4 * n_in));
+        constexpr int NWo = PAULI ? NW : 1;
+        const size_t smem = sizeof(OrbitTable<KW, CPLX>) * kOrbitWarps;
+        static bool attr_set = false;
+        if (!attr_set) {
+            CK(cudaFuncSetAttribute(orbit_process<NWo, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+            attr_set = true;
+        }
+        for (int attempt = 0; attempt < 8; attempt++) {
+            int rc = ensure_buf(ctx, ctx->buf[1 - active], store_bytes(KW, CPLX, out_cap));
+            if (rc) return rc;
+            Store dst = carve(ctx->buf[1 - active], KW, CPLX, out_cap);
+            CK(cudaMemsetAsync(ctx->d_oc, 0, sizeof(OrbitCounters), ctx->stream));
+            CK(cudaMemsetAsync(sc.gslots, 0xff, (sc.gmask + 1) * 8, ctx->stream));
+            {
+                PhaseScope ps(ctx, PH_ROT);
+                const int g = grid_for(ctx, n_in);
+                orbit_classify<NWo, CPLX><<<g, kBlock, 0, ctx->stream>>>(cur.v, n_in, dst.v, sc, ctx->d_oc, a);
+                OSTEP("orbit_classify");
+                orbit_group<KW><<<g, kBlock, 0, ctx->stream>>>(n_in, sc, ctx->d_oc);
+                OSTEP("orbit_group");
+                orbit_offsets<<<1, 1024, 0, ctx->stream>>>(sc, ctx->d_oc);
+                OSTEP("orbit_offsets");
+                orbit_scatter<<<g, kBlock, 0, ctx->stream>>>(n_in, sc);
+                OSTEP("orbit_scatter");
+                orbit_process<NWo, CPLX><<<ctx->num_sms * 2, 32 * kOrbitWarps, smem, ctx->stream>>>(
+                    cur.v, dst.v, sc, ctx->d_oc, a);
+                OSTEP("orbit_process");
+                ctx->prof.kernel_launches += 5;
+            }
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(ctx->h_oc, ctx->d_oc, sizeof(OrbitCounters), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            ctx->prof.syncs++;
+            if (ctx->profiling) drain_events(ctx);
+            OrbitCounters oc = *ctx->h_oc;
+            if (oc.error) return set_err(ctx, FFG_ERR_STATE, "orbit grouping index overrun");
+            if (oc.chk_code)
+                return set_err(ctx, FFG_ERR_STATE, "orbit self-check " + std::to_string(oc.chk_code) + " a=" +
+                                                       std::to_string(oc.chk_a) + " b=" + std::to_string(oc.chk_b) +
+                                                       " c=" + std::to_string(oc.chk_c));
+            if (oc.overflow & 1u) {
+                out_cap = pow2_at_least(oc.n_out + oc.n_out / 4 + 1024);
+                continue;
+            }
+            if (oc.nbig) {
+                const int br = exec_big_groups(dst.v, sc, a, oc.nbig);
+                if (br < 0) return br;
+                oc = *ctx->h_oc;
+                if (br == 2) {
+                    out_cap = pow2_at_least(oc.n_out + oc.n_out / 4 + 1024);
+                    continue;
+                }
+                ctx->prof.orbit_fallbacks += oc.nbig;  // groups done by the block-level pass
+            }
+            ctx->prof.orbit_max_group = std::max<int64_t>(ctx->prof.orbit_max_group, oc.max_members);
+            ctx->prof.orbit_batches++;
+            ctx->prof.orbit_groups += oc.ngroups;
+            // the output store becomes the live store
+            cur = dst;
+            cap = out_cap;
+            active = 1 - active;
+            index_valid = false;
+            DevCounters h = *ctx->h_ctr;
+            h.apps += (u64)k * n_in + oc.xapps;
+            h.emits += oc.emits;
+            const u64 before_trunc = n_in + oc.created;
+            if (before_trunc > h.peak) h.peak = before_trunc;
+            h.n = oc.n_out;
+            h.alive = oc.n_out;
+            *ctx->h_ctr = h;
+            CK(cudaMemcpyAsync(ctx->d_ctr, ctx->h_ctr, sizeof(DevCounters), cudaMemcpyHostToDevice, ctx->stream));
+            return FFG_OK;
+        }
+        return set_err(ctx, FFG_ERR_STATE, "orbit batch: output store kept overflowing");
+    }
+
+    // Pauli batched runs: long commuting runs go through the batch-orbit path,
+    // everything else through persistent per-gate runs.
+    int run_mixed(const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
+                  const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups,
+                  const std::vector<BatchInfo>& batches, int maxdeg) {
+        int rc = prepare_persistent(ops, rots, truncs, groups);
+        if (rc) return rc;
+        // batch gate table, in op order
+        std::vector<BatchGate> bg;
+        std::vector<int> gate_of_op(ops.size(), -1);
+        for (size_t o = 0; o < ops.size(); o++) {
+            if (ops[o].type != Op::GROUP) continue;
+            const GArgs& ga = groups[ops[o].idx];
+            BatchGate b{};
+            for (int w = 0; w < 4; w++) b.p[w] = ga.psub[1][w];
+            b.c = ga.c[0];
+            b.s = ga.s[0];
+            b.yP = ga.yP[0];
+            gate_of_op[o] = (int)bg.size();
+            bg.push_back(b);
+        }
+        rc = upload(ctx->d_bgates, ctx->bgates_cap, bg);
+        if (rc) return rc;
+        size_t pos = 0;  // next op to execute
+        for (const BatchInfo& b : batches) {
+            if (b.nrot < ctx->orbit_min_gates) continue;
+            const int end = b.trunc >= 0 ? b.trunc + 1 : b.first + b.nrot;
+            if (b.trunc >= 0 && ops[b.trunc].topk > 0) continue;
+            // ops before this batch go through the persistent kernel
+            if (pos < (size_t)b.first) {
+                rc = exec_persistent(pos, b.first);
+                if (rc) return rc;
+            }
+            rc = sync_counters();
+            if (rc) return rc;
+            if (ctx->h_ctr->n != ctx->h_ctr->alive) {
+                rc = compact_into(1 - active, cap);  // the orbit path reads a dense store
+                if (rc) return rc;
+                rc = sync_counters();
+                if (rc) return rc;
+            }
+            // split runs longer than the batch gate limit
+            int done = 0, st = FFG_OK;
+            while (done < b.nrot && st == FFG_OK) {
+                const int k = std::min(kMaxBatchGates, b.nrot - done);
+                const bool last = done + k == b.nrot;
+                const TruncArgs* t = (last && b.trunc >= 0) ? &truncs[ops[b.trunc].idx] : nullptr;
+                st = exec_orbit_batch(gate_of_op[b.first + done], k, t, maxdeg);
+                if (st == 1) break;
+                if (st) return st;
+                done += k;
+            }
+            if (st == 1) {
+                // a group too large for shared memory: finish this batch per gate
+                rc = exec_persistent(b.first + done, end);
+                if (rc) return rc;
+            }
+            pos = end;
+        }
+        if (pos < ops.size()) {
+            rc = exec_persistent(pos, ops.size());
+            if (rc) return rc;
+        }
+        return finish();
     }
 
     int extract(ffg_result** out, int kind, bool deterministic) {
@@ -786,7 +1116,7 @@ void add_groups(const ffg_pauli_gate* g, const std::vector<size_t>& run, const f
 void build_pauli_ops(const ffg_pauli_gate* g, size_t ng, const ffg_pauli_params& p, int nw,
                      std::vector<Op>& ops, std::vector<RotArgs>& rots, std::vector<TruncArgs>& truncs,
                      std::vector<int64_t>* batches, std::vector<GArgs>* groups = nullptr,
-                     int dmax = kGroupD) {
+                     int dmax = kGroupD, std::vector<BatchInfo>* binfo = nullptr) {
     int rot_count = 0;
     auto add_rot = [&](size_t i) {
         RotArgs a{};
@@ -853,14 +1183,18 @@ void build_pauli_ops(const ffg_pauli_gate* g, size_t ng, const ffg_pauli_params&
                     if (!ok) break;
                     e++;
                 }
+                const int first = (int)ops.size();
                 if (groups)
                     add_groups(g, std::vector<size_t>(buf.begin() + s, buf.begin() + e), p, nw, dmax,
                                ops, *groups);
                 else
                     for (size_t t = s; t < e; t++) add_rot(buf[t]);
+                const int nrot = (int)ops.size() - first;
                 if (batches) batches->push_back((int64_t)(e - s));
                 rot_count += (int)(e - s);
+                const size_t before = ops.size();
                 add_trunc(rot_count - 1);
+                if (binfo) binfo->push_back({first, nrot, ops.size() > before ? (int)before : -1});
                 s = e;
             }
             buf.clear();
@@ -900,13 +1234,18 @@ template <int KW, bool CPLX, bool PAULI>
 int run_engine(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im, size_t n,
                int on_device, const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
                const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups,
-               bool deterministic, ffg_result** out) {
+               bool deterministic, ffg_result** out, const std::vector<BatchInfo>* binfo = nullptr,
+               int maxdeg = 128) {
     Engine<KW, CPLX, PAULI> E(ctx);
     int rc = E.load(keys, re, im, n, on_device, 0);
     if (rc) return rc;
     bool has_topk = false;
     for (const Op& o : ops) has_topk = has_topk || (o.type == Op::TRUNC && o.topk > 0);
-    if (ctx->persistent && ctx->group_d <= 2 && !has_topk)
+    if (has_topk)
+        rc = E.run(ops, rots, truncs, groups);
+    else if (PAULI && binfo && ctx->orbit && ctx->persistent && ctx->group_d == 1)
+        rc = E.run_mixed(ops, rots, truncs, groups, *binfo, maxdeg);
+    else if (ctx->persistent && ctx->group_d <= 2)
         rc = E.run_persistent(ops, rots, truncs, groups);
     else
         rc = E.run(ops, rots, truncs, groups);
@@ -953,6 +1292,8 @@ int ffg_create(ffg_ctx** out, int device) {
     }
     if (const char* d = getenv("FFG_PERSISTENT")) ctx->persistent = atoi(d) != 0;
     if (const char* d = getenv("FFG_PERSIST_BPS")) ctx->persist_blocks_per_sm = std::max(1, atoi(d));
+    if (const char* d = getenv("FFG_ORBIT")) ctx->orbit = atoi(d) != 0;
+    if (const char* d = getenv("FFG_ORBIT_MIN")) ctx->orbit_min_gates = std::max(1, atoi(d));
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -961,6 +1302,8 @@ int ffg_create(ffg_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_part, 2 * kMaxParts * sizeof(double) + 2 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_hist, 256 * 8);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ps, sizeof(PersistState));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_oc, sizeof(OrbitCounters));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_oc, sizeof(OrbitCounters));
     if (e != cudaSuccess) {
         fprintf(stderr, "ffg_create: %s\n", cudaGetErrorString(e));
         ffg_destroy(ctx);
@@ -986,6 +1329,11 @@ int ffg_destroy(ffg_ctx* ctx) {
     if (ctx->d_mrots) cudaFree(ctx->d_mrots);
     if (ctx->d_truncs) cudaFree(ctx->d_truncs);
     if (ctx->d_groups2) cudaFree(ctx->d_groups2);
+    if (ctx->d_bgates) cudaFree(ctx->d_bgates);
+    if (ctx->d_oscratch) cudaFree(ctx->d_oscratch);
+    if (ctx->bigpool.p) cudaFree(ctx->bigpool.p);
+    if (ctx->d_oc) cudaFree(ctx->d_oc);
+    if (ctx->h_oc) cudaFreeHost(ctx->h_oc);
     if (ctx->d_ctr) cudaFree(ctx->d_ctr);
     if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
     for (auto e : ctx->free_events) cudaEventDestroy(e);
@@ -1061,7 +1409,9 @@ int ffg_pauli_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, co
         std::vector<RotArgs> rots;
         std::vector<TruncArgs> truncs;
         std::vector<GArgs> groups;
-        build_pauli_ops(gates, ngates, *params, nw, ops, rots, truncs, nullptr, &groups, ctx->group_d);
+        std::vector<BatchInfo> binfo;
+        build_pauli_ops(gates, ngates, *params, nw, ops, rots, truncs, nullptr, &groups, ctx->group_d,
+                        &binfo);
         int64_t nrot = 0;
         for (const auto& gr : groups) nrot += gr.ng;
         ctx->prof.n_gates = nrot;
@@ -1069,13 +1419,17 @@ int ffg_pauli_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, co
         if (rc) return rc;
         const bool det = params->deterministic != 0;
         if (nw == 1 && !cplx)
-            rc = run_engine<2, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out);
+            rc = run_engine<2, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out,
+                                                &binfo, params->maxdegree);
         else if (nw == 1)
-            rc = run_engine<2, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out);
+            rc = run_engine<2, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out,
+                                                &binfo, params->maxdegree);
         else if (!cplx)
-            rc = run_engine<4, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out);
+            rc = run_engine<4, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out,
+                                                &binfo, params->maxdegree);
         else
-            rc = run_engine<4, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out);
+            rc = run_engine<4, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out,
+                                                &binfo, params->maxdegree);
         ctx->prof.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return rc;
     } catch (const std::exception& ex) {

@@ -1,0 +1,714 @@
+// Batch-orbit processing of a run of mutually commuting Pauli rotations.
+//
+// Within a commuting batch (src/pauli/propagate.h:272-291) a term Q is acted on
+// only by the gates A(Q) = {t : Q anticommutes with P_t}, and every product
+// Q * P_t (t in A) has the same set A (the axes commute).  The gates therefore
+// never pair terms whose sets A differ, nor terms that differ outside the
+// bits U_A touched by the axes of A.  Terms are grouped by the key
+// (A, Q & ~U_A); each group is a union of orbits Q * <P_t : t in A> and is
+// processed on its own, gate by gate in batch order, with exactly the
+// per-gate arithmetic, degree filter and creation rule of the reference
+// (src/pauli/propagate.h:71-89).  The per-gate update of a group only involves
+// its own members, so the result is bit-identical to applying the whole
+// store gate by gate, while the work scales with the number of member updates
+// rather than with (gates x store size).
+//
+// Kernels of one batch:
+//   orbit_classify   A(Q) and the group key of every input term; terms with
+//                    A = {} are final and go straight to the output store
+//   orbit_group      representative of every term's group (hash of the key)
+//   orbit_count / orbit_offsets / orbit_scatter
+//                    group members made contiguous
+//   orbit_process    one warp per group: members in a shared-memory table,
+//                    gates applied in order, survivors of the batch-end
+//                    truncation appended to the output store
+// A group whose member count would exceed kOrbitCap stops the batch (the
+// host falls back to per-gate passes for it); so does an output store that
+// would overflow (the host grows it and runs the batch again).
+#pragma once
+#include "ffg_kernels.cuh"
+
+namespace ffg {
+
+constexpr int kMaxBatchGates = 256;        // gates per orbit batch (longer runs are split)
+constexpr int kAW = kMaxBatchGates / 64;   // words of a gate-subset mask
+constexpr int kOrbitCap = 512;             // members of one group held in shared memory
+constexpr int kOrbitWarps = 4;             // groups in flight per block
+
+struct BatchGate {
+    u64 p[4];     // axis planes in store order (the NW x words, then the NW z words)
+    double c, s;
+    int yP;
+    int pad;
+};
+
+struct OrbitScratch {
+    u64* amask;    // [kAW][cap_in] gate-subset mask of each input term
+    u64* gkey;     // [4][cap_in] key outside U_A
+    u32* rep;      // [cap_in] representative of the term's group (0xffffffff = final)
+    u32* cnt;      // [cap_in] members of the group represented by a term
+    u32* off;      // [cap_in] first position of that group in `order`
+    u32* fill;     // [cap_in]
+    u32* order;    // [cap_in] input positions grouped
+    u32* groups;   // [cap_in] list of representatives
+    u32* big;      // [cap_in] representatives of groups too large for a warp table
+    u64* gslots;   // [2*cap_in] group index: (fingerprint << 32) | representative
+    u64 gmask;
+    u64 cap_in;
+};
+
+struct OrbitCounters {
+    u64 n_out;         // entries written to the output store
+    u64 created;       // members created inside the batch
+    u64 xapps;         // sum over created members of the batch gates after their creation
+    u64 emits;
+    u32 ngroups;
+    u32 overflow;      // 1: output store too small, 2: a group outgrew kOrbitCap
+    u32 error;
+    u32 max_members;   // largest group seen (members at the end, or on input when too large)
+    u32 nbig;          // groups left for the block-level pass (list in OrbitScratch::big)
+    u32 big_overflow;  // a block-level group outgrew its region
+    u32 chk_code;      // self-check builds: first failed check (0 = none)
+    u32 chk_a, chk_b, chk_c;
+};
+
+#ifdef FFG_ORBIT_CHECK
+#define OCHK(cond, code, a_, b_, c_)                                              \
+    if (!(cond)) {                                                               \
+        if (atomicCAS(&oc->chk_code, 0u, (u32)(code)) == 0u) {                   \
+            oc->chk_a = (u32)(a_);                                               \
+            oc->chk_b = (u32)(b_);                                               \
+            oc->chk_c = (u32)(c_);                                               \
+        }                                                                        \
+        continue;                                                                \
+    }
+#else
+#define OCHK(cond, code, a_, b_, c_)
+#endif
+
+struct OrbitBatchArgs {
+    const BatchGate* gates;  // k gates of the batch, application order
+    int k;
+    int maxdeg;
+    // fused batch-end truncation
+    int thr;
+    double tau;
+    int max_xweight;
+};
+
+template <int NW, bool CPLX>
+__device__ __forceinline__ bool survives(const u64* key, cplx c, const OrbitBatchArgs& a) {
+    if (a.thr) {
+        const bool small = CPLX ? abs_le(c.re, c.im, a.tau) : (fabs(c.re) <= a.tau);
+        if (small) return false;
+    }
+    if (a.max_xweight >= 0) {
+        int xw = 0;
+#pragma unroll
+        for (int w = 0; w < NW; w++) xw += __popcll(key[w]);
+        if (xw > a.max_xweight) return false;
+    }
+    return true;
+}
+
+template <int KW, bool CPLX>
+__device__ __forceinline__ void out_append(const StoreView& o, OrbitCounters* oc, const u64* key, cplx c) {
+    const u64 pos = atomicAdd(&oc->n_out, 1ull);
+    if (pos >= o.cap) {
+        atomicOr(&oc->overflow, 1u);
+        return;
+    }
+#pragma unroll
+    for (int w = 0; w < KW; w++) o.key[(u64)w * o.cap + pos] = key[w];
+    o.re[pos] = c.re;
+    if (CPLX) o.im[pos] = c.im;
+    o.dead[pos] = 0;
+}
+
+// A(Q) for every input term; group key; final terms go to the output.
+template <int NW, bool CPLX>
+__global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, u64 n_in, StoreView out,
+                                                         OrbitScratch sc, OrbitCounters* oc,
+                                                         OrbitBatchArgs a) {
+    constexpr int KW = 2 * NW;
+    __shared__ u64 gp[kMaxBatchGates][KW];
+    for (int t = threadIdx.x; t < a.k; t += blockDim.x)
+        for (int w = 0; w < KW; w++) gp[t][w] = a.gates[t].p[w];
+    __syncthreads();
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += stride) {
+        u64 q[KW];
+        load_key<KW>(in, i, q);
+        u64 A[kAW] = {};
+        u64 U[KW] = {};
+        for (int t = 0; t < a.k; t++) {
+            u64 par = 0;
+#pragma unroll
+            for (int w = 0; w < NW; w++) par ^= (q[w] & gp[t][NW + w]) ^ (q[NW + w] & gp[t][w]);
+            if (__popcll(par) & 1) {
+                A[t >> 6] |= 1ull << (t & 63);
+#pragma unroll
+                for (int w = 0; w < KW; w++) U[w] |= gp[t][w];
+            }
+        }
+        bool any = false;
+#pragma unroll
+        for (int w = 0; w < kAW; w++) any = any || A[w];
+        if (!any) {
+            sc.rep[i] = 0xffffffffu;
+            const cplx c = load_coef<CPLX>(in, i);
+            if (survives<NW, CPLX>(q, c, a)) out_append<KW, CPLX>(out, oc, q, c);
+            continue;
+        }
+#pragma unroll
+        for (int w = 0; w < kAW; w++) sc.amask[(u64)w * sc.cap_in + i] = A[w];
+#pragma unroll
+        for (int w = 0; w < KW; w++) sc.gkey[(u64)w * sc.cap_in + i] = q[w] & ~U[w];
+        sc.cnt[i] = 0;
+        sc.fill[i] = 0;
+        sc.rep[i] = 0xfffffffeu;  // grouped in the next pass
+    }
+}
+
+template <int KW>
+__device__ __forceinline__ u64 group_hash(const OrbitScratch& sc, u64 i) {
+    u64 h = 0x51ed270b27e41b3bull;
+#pragma unroll
+    for (int w = 0; w < kAW; w++) h = mix64(h ^ sc.amask[(u64)w * sc.cap_in + i]);
+#pragma unroll
+    for (int w = 0; w < KW; w++) h = mix64(h ^ sc.gkey[(u64)w * sc.cap_in + i]);
+    return h;
+}
+
+template <int KW>
+__device__ __forceinline__ bool same_group(const OrbitScratch& sc, u64 i, u64 j) {
+#pragma unroll
+    for (int w = 0; w < kAW; w++)
+        if (sc.amask[(u64)w * sc.cap_in + i] != sc.amask[(u64)w * sc.cap_in + j]) return false;
+#pragma unroll
+    for (int w = 0; w < KW; w++)
+        if (sc.gkey[(u64)w * sc.cap_in + i] != sc.gkey[(u64)w * sc.cap_in + j]) return false;
+    return true;
+}
+
+// representative of each term's group: the term that claims the index slot
+template <int KW>
+__global__ void __launch_bounds__(kBlock) orbit_group(u64 n_in, OrbitScratch sc, OrbitCounters* oc) {
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += stride) {
+        if (sc.rep[i] == 0xffffffffu) continue;
+        const u64 h = group_hash<KW>(sc, i);
+        const u32 fp = (u32)(h >> 32);
+        u64 pos = h & sc.gmask;
+        u32 rep = 0xffffffffu;
+        for (u64 probe = 0; probe <= sc.gmask; probe++) {
+            u64 e = __ldcg(&sc.gslots[pos]);
+            if (e == kEmptySlot) {
+                e = atomicCAS(&sc.gslots[pos], kEmptySlot, ((u64)fp << 32) | i);
+                if (e == kEmptySlot) {
+                    rep = (u32)i;
+                    break;
+                }
+            }
+            if ((u32)(e >> 32) == fp && same_group<KW>(sc, i, (u32)e)) {
+                rep = (u32)e;
+                break;
+            }
+            pos = (pos + 1) & sc.gmask;
+        }
+        if (rep == 0xffffffffu) {
+            atomicOr(&oc->error, 1u);
+            rep = (u32)i;
+        }
+        sc.rep[i] = rep;
+        atomicAdd(&sc.cnt[rep], 1u);
+        if (rep == (u32)i) {
+            const u32 g = atomicAdd(&oc->ngroups, 1u);
+            sc.groups[g] = (u32)i;
+        }
+    }
+}
+
+// first member position of every group (groups listed in sc.groups)
+__global__ void __launch_bounds__(1024) orbit_offsets(OrbitScratch sc, OrbitCounters* oc) {
+    const u32 ng = *(volatile u32*)&oc->ngroups;
+    __shared__ u32 carry;
+    __shared__ u32 wt[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (u32 base = 0; base < ng; base += blockDim.x) {
+        const u32 g = base + threadIdx.x;
+        const u32 v = g < ng ? sc.cnt[sc.groups[g]] : 0u;
+        u32 x = v;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wt[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            u32 w = lane < (int)(blockDim.x >> 5) ? wt[lane] : 0u;
+            for (int o = 1; o < 32; o <<= 1) {
+                const u32 y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            wt[lane] = w;
+        }
+        __syncthreads();
+        const u32 incl = x + (wid > 0 ? wt[wid - 1] : 0u);
+        if (g < ng) sc.off[sc.groups[g]] = carry + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += incl;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) orbit_scatter(u64 n_in, OrbitScratch sc) {
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += stride) {
+        const u32 r = sc.rep[i];
+        if (r == 0xffffffffu) continue;
+        const u32 p = sc.off[r] + atomicAdd(&sc.fill[r], 1u);
+        sc.order[p] = (u32)i;
+    }
+}
+
+// --- group processing: one warp per group ----------------------------------
+template <int KW, bool CPLX>
+struct OrbitTable {
+    u64 key[kOrbitCap][KW];
+    double re[kOrbitCap];
+    double im[CPLX ? kOrbitCap : 1];
+    unsigned short slot[2 * kOrbitCap];  // index of members, 0xffff = empty
+    unsigned int cnt;                     // members in the table
+    unsigned int flag;                    // the group outgrew the table
+};
+
+template <int KW>
+__device__ __forceinline__ u32 small_hash(const u64* k) {
+    u64 h = mix64(k[0] ^ 0x2545f4914f6cdd1dull);
+#pragma unroll
+    for (int w = 1; w < KW; w++) h = mix64(h ^ k[w]);
+    return (u32)h;
+}
+
+// member index of key k or -1 (lanes of one warp share the table)
+template <int KW, bool CPLX>
+__device__ __forceinline__ int table_find(const OrbitTable<KW, CPLX>& T, const u64* k) {
+    u32 pos = small_hash<KW>(k) & (2 * kOrbitCap - 1);
+    for (int probe = 0; probe < 2 * kOrbitCap; probe++) {
+        const unsigned short m = ((volatile unsigned short*)T.slot)[pos];
+        if (m == 0xffff) return -1;
+        bool eq = true;
+#pragma unroll
+        for (int w = 0; w < KW; w++) eq = eq && T.key[m][w] == k[w];
+        if (eq) return m;
+        pos = (pos + 1) & (2 * kOrbitCap - 1);
+    }
+    return -1;
+}
+
+template <int KW, bool CPLX>
+__device__ __forceinline__ void table_insert(OrbitTable<KW, CPLX>& T, const u64* k, unsigned short m) {
+    u32 pos = small_hash<KW>(k) & (2 * kOrbitCap - 1);
+    for (int probe = 0; probe < 2 * kOrbitCap; probe++) {
+        unsigned int* word = (unsigned int*)&T.slot[pos & ~1u];
+        const int hi = pos & 1;
+        unsigned int old = *(volatile unsigned int*)word;
+        for (;;) {
+            const unsigned short cur = hi ? (unsigned short)(old >> 16) : (unsigned short)(old & 0xffff);
+            if (cur != 0xffff) break;
+            const unsigned int nw = hi ? ((old & 0x0000ffffu) | ((u32)m << 16)) : ((old & 0xffff0000u) | m);
+            const unsigned int seen = atomicCAS(word, old, nw);
+            if (seen == old) return;
+            old = seen;
+        }
+        pos = (pos + 1) & (2 * kOrbitCap - 1);
+    }
+}
+
+template <int NW, bool CPLX>
+__global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, StoreView out, OrbitScratch sc,
+                                                                  OrbitCounters* oc, OrbitBatchArgs a) {
+    constexpr int KW = 2 * NW;
+    extern __shared__ unsigned char smem[];
+    OrbitTable<KW, CPLX>* tables = (OrbitTable<KW, CPLX>*)smem;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    OrbitTable<KW, CPLX>& T = tables[warp];
+    const u32 ng = *(volatile u32*)&oc->ngroups;
+    long long emits = 0, created = 0, xapps = 0;
+    for (u32 g = blockIdx.x * kOrbitWarps + warp; g < ng; g += gridDim.x * kOrbitWarps) {
+        long long g_emits = 0, g_created = 0, g_xapps = 0;
+        OCHK(g < sc.cap_in, 13, g, ng, 0)
+        const u32 rep = sc.groups[g];
+        OCHK(rep < sc.cap_in, 14, rep, g, ng)
+        const u32 m0 = sc.cnt[rep];
+        const u32 base = sc.off[rep];
+        if (m0 > kOrbitCap) {
+            if (lane == 0) {
+                sc.big[atomicAdd(&oc->nbig, 1u)] = rep;
+                atomicMax(&oc->max_members, m0);
+            }
+            continue;
+        }
+        // load members
+        for (int s = lane; s < 2 * kOrbitCap; s += 32) T.slot[s] = 0xffff;
+        __syncwarp();
+        for (u32 m = lane; m < m0; m += 32) {
+            OCHK((u64)base + m < sc.cap_in, 11, base, m, rep)
+            const u32 i = sc.order[base + m];
+            OCHK(i < in.cap, 12, i, m, rep)
+#pragma unroll
+            for (int w = 0; w < KW; w++) T.key[m][w] = in.key[(u64)w * in.cap + i];
+            T.re[m] = in.re[i];
+            if (CPLX) T.im[m] = in.im[i];
+            table_insert<KW, CPLX>(T, T.key[m], (unsigned short)m);
+        }
+        if (lane == 0) {
+            T.cnt = m0;
+            T.flag = 0;
+        }
+        __syncwarp();
+        // gates of A in batch order
+        u64 A[kAW];
+#pragma unroll
+        for (int w = 0; w < kAW; w++) A[w] = sc.amask[(u64)w * sc.cap_in + rep];
+        for (int wd = 0; wd < kAW; wd++) {
+            u64 bits = A[wd];
+            while (bits) {
+                const int t = 64 * wd + __ffsll((long long)bits) - 1;
+                bits &= bits - 1;
+                const BatchGate G = a.gates[t];
+                u64 P[KW];
+#pragma unroll
+                for (int w = 0; w < KW; w++) P[w] = G.p[w];
+                const cplx isin = {0.0, G.s};
+                const int cnt0 = (int)*(volatile unsigned int*)&T.cnt;
+                __syncwarp();
+                for (int m = lane; m < cnt0; m += 32) {
+                    u64 q[KW], k[KW];
+#pragma unroll
+                    for (int w = 0; w < KW; w++) {
+                        q[w] = T.key[m][w];
+                        k[w] = q[w] ^ P[w];
+                    }
+                    int yQ = 0, yK = 0, zxQ = 0, zxK = 0, dQ = 0, dK = 0;
+#pragma unroll
+                    for (int w = 0; w < NW; w++) {
+                        yQ += __popcll(q[w] & q[NW + w]);
+                        yK += __popcll(k[w] & k[NW + w]);
+                        zxQ += __popcll(P[NW + w] & q[w]);
+                        zxK += __popcll(P[NW + w] & k[w]);
+                        dQ += __popcll(q[w] | q[NW + w]);
+                        dK += __popcll(k[w] | k[NW + w]);
+                    }
+                    const int jQ = G.yP + yQ + 2 * zxQ - yK;  // P*Q -> K
+                    const int jK = G.yP + yK + 2 * zxK - yQ;  // P*K -> Q
+                    const cplx ci = {T.re[m], CPLX ? T.im[m] : 0.0};
+                    const int j = table_find<KW, CPLX>(T, k);
+                    if (j >= 0 && j < cnt0) {
+                        if (j < m) continue;  // the pair belongs to member j
+                        const cplx cj = {T.re[j], CPLX ? T.im[j] : 0.0};
+                        cplx ni = cscale(ci, G.c), nj = cscale(cj, G.c);
+                        if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
+                        if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
+                        g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
+                        T.re[m] = ni.re;
+                        T.re[j] = nj.re;
+                        if (CPLX) {
+                            T.im[m] = ni.im;
+                            T.im[j] = nj.im;
+                        }
+                    } else {
+                        const cplx ni = cscale(ci, G.c);
+                        T.re[m] = ni.re;
+                        if (CPLX) T.im[m] = ni.im;
+                        if (dK <= a.maxdeg) {
+                            g_emits++;
+                            const cplx nv = cadd({0.0, 0.0}, cmul(cmul(ci, isin), ipow(jQ)));
+                            const unsigned int idx = atomicAdd(&T.cnt, 1u);
+                            if (idx >= (unsigned int)kOrbitCap) {
+                                atomicExch(&T.flag, 1u);
+                            } else {
+#pragma unroll
+                                for (int w = 0; w < KW; w++) T.key[idx][w] = k[w];
+                                T.re[idx] = nv.re;
+                                if (CPLX) T.im[idx] = nv.im;
+                                __threadfence_block();
+                                table_insert<KW, CPLX>(T, k, (unsigned short)idx);
+                                g_created++;
+                                g_xapps += a.k - 1 - t;
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+                if (*(volatile unsigned int*)&T.flag) break;
+            }
+            if (*(volatile unsigned int*)&T.flag) break;
+        }
+        __syncwarp();
+        if (*(volatile unsigned int*)&T.flag) {
+            if (lane == 0) sc.big[atomicAdd(&oc->nbig, 1u)] = rep;
+            continue;
+        }
+        emits += g_emits;
+        created += g_created;
+        xapps += g_xapps;
+        // survivors of the batch-end truncation go to the output store
+        const int cnt = (int)*(volatile unsigned int*)&T.cnt;
+        if (lane == 0) atomicMax(&oc->max_members, (u32)cnt);
+        for (int m = lane; m < cnt; m += 32) {
+            const cplx c = {T.re[m], CPLX ? T.im[m] : 0.0};
+            if (survives<NW, CPLX>(T.key[m], c, a)) out_append<KW, CPLX>(out, oc, T.key[m], c);
+        }
+        __syncwarp();
+    }
+    // block totals
+    for (int o = 16; o > 0; o >>= 1) {
+        emits += __shfl_down_sync(0xffffffffu, emits, o);
+        created += __shfl_down_sync(0xffffffffu, created, o);
+        xapps += __shfl_down_sync(0xffffffffu, xapps, o);
+    }
+    if (lane == 0) {
+        if (emits) atomicAdd(&oc->emits, (u64)emits);
+        if (created) atomicAdd(&oc->created, (u64)created);
+        if (xapps) atomicAdd(&oc->xapps, (u64)xapps);
+    }
+}
+
+// --- groups too large for a warp: one block per group, table in global memory
+struct BigPool {
+    char* base;      // regions of region_bytes each
+    u64 region_bytes;
+    u32 rcap;        // members per region (power of two)
+    u32* retry;      // representatives of groups that outgrew their region
+    u32* nretry;
+};
+
+template <int KW, bool CPLX>
+struct BigRegion {
+    u64* key;      // [KW][rcap]
+    double* re;
+    double* im;
+    u32* slot;     // [2*rcap], 0xffffffff = empty
+    u32* cnt;
+    u32* flag;
+};
+
+template <int KW, bool CPLX>
+__device__ __forceinline__ BigRegion<KW, CPLX> big_region(const BigPool& bp, u32 r) {
+    BigRegion<KW, CPLX> g;
+    char* p = bp.base + (u64)r * bp.region_bytes;
+    g.key = (u64*)p;
+    p += (u64)KW * bp.rcap * 8;
+    g.re = (double*)p;
+    p += (u64)bp.rcap * 8;
+    g.im = (double*)p;
+    if (CPLX) p += (u64)bp.rcap * 8;
+    g.slot = (u32*)p;
+    p += (u64)2 * bp.rcap * 4;
+    g.cnt = (u32*)p;
+    g.flag = g.cnt + 1;
+    return g;
+}
+
+template <int KW, bool CPLX>
+__device__ __forceinline__ int big_find(const BigRegion<KW, CPLX>& G, u32 rcap, const u64* k) {
+    const u32 mask = 2 * rcap - 1;
+    u32 pos = small_hash<KW>(k) & mask;
+    for (u32 probe = 0; probe <= mask; probe++) {
+        const u32 m = __ldcg(&G.slot[pos]);
+        if (m == 0xffffffffu) return -1;
+#ifdef FFG_ORBIT_CHECK
+        if (m >= rcap) return (int)0x7fffffff;
+#endif
+        bool eq = true;
+#pragma unroll
+        for (int w = 0; w < KW; w++) eq = eq && __ldcg(&G.key[(u64)w * rcap + m]) == k[w];
+        if (eq) return (int)m;
+        pos = (pos + 1) & mask;
+    }
+    return -1;
+}
+
+template <int KW, bool CPLX>
+__device__ __forceinline__ void big_insert(const BigRegion<KW, CPLX>& G, u32 rcap, const u64* k, u32 m) {
+    const u32 mask = 2 * rcap - 1;
+    u32 pos = small_hash<KW>(k) & mask;
+    for (u32 probe = 0; probe <= mask; probe++) {
+        if (atomicCAS(&G.slot[pos], 0xffffffffu, m) == 0xffffffffu) return;
+        pos = (pos + 1) & mask;
+    }
+}
+
+template <int NW, bool CPLX>
+__global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreView out, OrbitScratch sc,
+                                                          OrbitCounters* oc, OrbitBatchArgs a, BigPool bp,
+                                                          const u32* list, u32 nlist) {
+    constexpr int KW = 2 * NW;
+    __shared__ long long red[3][32];
+    long long emits = 0, created = 0, xapps = 0;
+    for (u32 gi = blockIdx.x; gi < nlist; gi += gridDim.x) {
+        OCHK(gi < sc.cap_in, 8, gi, nlist, 0)
+        const u32 rep = list[gi];
+        OCHK(rep < sc.cap_in, 9, rep, gi, nlist)
+        const BigRegion<KW, CPLX> G = big_region<KW, CPLX>(bp, blockIdx.x);
+        const u32 rcap = bp.rcap;
+        const u32 m0 = sc.cnt[rep];
+        const u32 base = sc.off[rep];
+        for (u32 s2 = threadIdx.x; s2 < 2 * rcap; s2 += blockDim.x) G.slot[s2] = 0xffffffffu;
+        if (threadIdx.x == 0) {
+            *G.cnt = m0;
+            *G.flag = m0 > rcap ? 1u : 0u;
+        }
+        __syncthreads();
+        if (*(volatile u32*)G.flag) {
+            if (threadIdx.x == 0) bp.retry[atomicAdd(bp.nretry, 1u)] = rep;
+            __syncthreads();
+            continue;
+        }
+        for (u32 m = threadIdx.x; m < m0; m += blockDim.x) {
+            OCHK((u64)base + m < sc.cap_in, 1, base, m, rep)
+            const u32 i = sc.order[base + m];
+            OCHK(i < in.cap, 2, i, m, rep)
+            OCHK(m < rcap, 3, m, rcap, rep)
+            u64 k[KW];
+#pragma unroll
+            for (int w = 0; w < KW; w++) {
+                k[w] = in.key[(u64)w * in.cap + i];
+                G.key[(u64)w * rcap + m] = k[w];
+            }
+            G.re[m] = in.re[i];
+            if (CPLX) G.im[m] = in.im[i];
+            __threadfence_block();
+            big_insert<KW, CPLX>(G, rcap, k, m);
+        }
+        __syncthreads();
+        long long g_emits = 0, g_created = 0, g_xapps = 0;
+        bool stop = false;
+        for (int wd = 0; wd < kAW && !stop; wd++) {
+            u64 bits = sc.amask[(u64)wd * sc.cap_in + rep];
+            while (bits && !stop) {
+                const int t = 64 * wd + __ffsll((long long)bits) - 1;
+                bits &= bits - 1;
+                const BatchGate Gt = a.gates[t];
+                u64 P[KW];
+#pragma unroll
+                for (int w = 0; w < KW; w++) P[w] = Gt.p[w];
+                const cplx isin = {0.0, Gt.s};
+                const u32 cnt0 = *(volatile u32*)G.cnt;
+                __syncthreads();
+                for (u32 m = threadIdx.x; m < cnt0; m += blockDim.x) {
+                    OCHK(m < rcap, 4, m, cnt0, t)
+                    OCHK(t < a.k, 5, t, a.k, rep)
+                    u64 q[KW], k[KW];
+#pragma unroll
+                    for (int w = 0; w < KW; w++) {
+                        q[w] = __ldcg(&G.key[(u64)w * rcap + m]);
+                        k[w] = q[w] ^ P[w];
+                    }
+                    int yQ = 0, yK = 0, zxQ = 0, zxK = 0, dQ = 0, dK = 0;
+#pragma unroll
+                    for (int w = 0; w < NW; w++) {
+                        yQ += __popcll(q[w] & q[NW + w]);
+                        yK += __popcll(k[w] & k[NW + w]);
+                        zxQ += __popcll(P[NW + w] & q[w]);
+                        zxK += __popcll(P[NW + w] & k[w]);
+                        dQ += __popcll(q[w] | q[NW + w]);
+                        dK += __popcll(k[w] | k[NW + w]);
+                    }
+                    const int jQ = Gt.yP + yQ + 2 * zxQ - yK;
+                    const int jK = Gt.yP + yK + 2 * zxK - yQ;
+                    const cplx ci = {__ldcg(&G.re[m]), CPLX ? __ldcg(&G.im[m]) : 0.0};
+                    const int j = big_find<KW, CPLX>(G, rcap, k);
+                    OCHK(j < (int)rcap, 6, j, rcap, m)
+                    if (j >= 0 && (u32)j < cnt0) {
+                        if ((u32)j < m) continue;
+                        const cplx cj = {__ldcg(&G.re[j]), CPLX ? __ldcg(&G.im[j]) : 0.0};
+                        cplx ni = cscale(ci, Gt.c), nj = cscale(cj, Gt.c);
+                        if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
+                        if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
+                        g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
+                        G.re[m] = ni.re;
+                        G.re[j] = nj.re;
+                        if (CPLX) {
+                            G.im[m] = ni.im;
+                            G.im[j] = nj.im;
+                        }
+                    } else {
+                        const cplx ni = cscale(ci, Gt.c);
+                        G.re[m] = ni.re;
+                        if (CPLX) G.im[m] = ni.im;
+                        if (dK <= a.maxdeg) {
+                            g_emits++;
+                            const cplx nv = cadd({0.0, 0.0}, cmul(cmul(ci, isin), ipow(jQ)));
+                            const u32 idx = atomicAdd(G.cnt, 1u);
+                            if (idx >= rcap) {
+                                atomicExch(G.flag, 1u);
+                            } else {
+#pragma unroll
+                                for (int w = 0; w < KW; w++) G.key[(u64)w * rcap + idx] = k[w];
+                                G.re[idx] = nv.re;
+                                if (CPLX) G.im[idx] = nv.im;
+                                __threadfence_block();
+                                big_insert<KW, CPLX>(G, rcap, k, idx);
+                                g_created++;
+                                g_xapps += a.k - 1 - t;
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+                stop = *(volatile u32*)G.flag != 0;
+            }
+        }
+        __syncthreads();
+        if (*(volatile u32*)G.flag) {
+            if (threadIdx.x == 0) bp.retry[atomicAdd(bp.nretry, 1u)] = rep;
+            __syncthreads();
+            continue;
+        }
+        emits += g_emits;
+        created += g_created;
+        xapps += g_xapps;
+        const u32 cnt = *(volatile u32*)G.cnt;
+        if (threadIdx.x == 0) atomicMax(&oc->max_members, cnt);
+        for (u32 m = threadIdx.x; m < cnt; m += blockDim.x) {
+            OCHK(m < rcap, 7, m, cnt, rcap)
+            u64 k[KW];
+#pragma unroll
+            for (int w = 0; w < KW; w++) k[w] = __ldcg(&G.key[(u64)w * rcap + m]);
+            const cplx c = {__ldcg(&G.re[m]), CPLX ? __ldcg(&G.im[m]) : 0.0};
+            if (survives<NW, CPLX>(k, c, a)) out_append<KW, CPLX>(out, oc, k, c);
+        }
+        __syncthreads();
+    }
+    // block totals
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        emits += __shfl_down_sync(0xffffffffu, emits, o);
+        created += __shfl_down_sync(0xffffffffu, created, o);
+        xapps += __shfl_down_sync(0xffffffffu, xapps, o);
+    }
+    if (lane == 0) {
+        red[0][wid] = emits;
+        red[1][wid] = created;
+        red[2][wid] = xapps;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long e = 0, c = 0, x = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            e += red[0][w];
+            c += red[1][w];
+            x += red[2][w];
+        }
+        if (e) atomicAdd(&oc->emits, (u64)e);
+        if (c) atomicAdd(&oc->created, (u64)c);
+        if (x) atomicAdd(&oc->xapps, (u64)x);
+    }
+}
+
+}  // namespace ffg

@@ -112,6 +112,10 @@ typedef struct {
     int64_t regrows;          /* capacity growths (each replays the pending gates) */
     int64_t compactions;
     int64_t kernel_launches;  /* kernels launched by the propagation */
+    int64_t orbit_batches;    /* commuting runs processed orbit by orbit */
+    int64_t orbit_fallbacks;  /* groups too large for a warp table (done by the block-level pass) */
+    int64_t orbit_groups;     /* groups processed */
+    int64_t orbit_max_group;  /* largest group (members) */
 } ffg_profile;
 
 /* -------------------------------------------------------------------------- */
