@@ -146,6 +146,7 @@ struct ffg_ctx {
     size_t groups2_cap = 0;
     bool orbit = true;          // batch-orbit path for long commuting runs (FFG_ORBIT=0 disables)
     int orbit_min_gates = 4;    // shortest run sent to the batch-orbit path
+    int orbit_route_big = 10;   // |A| from which a group skips the warp-level pass (FFG_ORBIT_ROUTE)
     BatchGate* d_bgates = nullptr;
     size_t bgates_cap = 0;
     char* d_oscratch = nullptr;
@@ -763,27 +764,41 @@ struct Engine {
         constexpr int NWo = PAULI ? NW : 1;
         u32* list = sc.big;
         u32* other = retry_list;
-        u64 rcap = 1ull << 16;
+        bool smem_pass = true;  // first a shared-memory table per block, then global regions
+        u64 rcap = 1ull << 14;
+        const size_t tb = block_table_bytes<KW, CPLX>();
+        static bool attr_set = false;
+        if (!attr_set) {
+            CK(cudaFuncSetAttribute(orbit_process_big<NWo, CPLX, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb));
+            attr_set = true;
+        }
         while (nbig > 0) {
             const u32 grid = std::min<u32>(nbig, (u32)ctx->num_sms);
-            const u64 region = align256((size_t)KW * rcap * 8 + rcap * 8 * (CPLX ? 2 : 1) + 2 * rcap * 4 + 8);
-            int rc = ensure_buf(ctx, ctx->bigpool, region * grid);
-            if (rc) return rc;
             BigPool bp{};
-            bp.base = ctx->bigpool.p;
-            bp.region_bytes = region;
-            bp.rcap = (u32)rcap;
             bp.retry = other;
             bp.nretry = nretry;
+            if (!smem_pass) {
+                const u64 region =
+                    align256((size_t)KW * rcap * 8 + rcap * 8 * (CPLX ? 2 : 1) + 2 * rcap * 4 + 8);
+                int rc = ensure_buf(ctx, ctx->bigpool, region * grid);
+                if (rc) return rc;
+                bp.base = ctx->bigpool.p;
+                bp.region_bytes = region;
+                bp.rcap = (u32)rcap;
+            }
             CK(cudaMemsetAsync(nretry, 0, 4, ctx->stream));
             {
                 PhaseScope ps(ctx, PH_ROT);
-                orbit_process_big<NWo, CPLX><<<grid, 1024, 0, ctx->stream>>>(cur.v, out, sc, ctx->d_oc, a, bp,
-                                                                             list, nbig);
+                if (smem_pass)
+                    orbit_process_big<NWo, CPLX, true><<<grid, 1024, tb, ctx->stream>>>(cur.v, out, sc, ctx->d_oc,
+                                                                                      a, bp, list, nbig);
+                else
+                    orbit_process_big<NWo, CPLX, false><<<grid, 1024, 0, ctx->stream>>>(cur.v, out, sc, ctx->d_oc,
+                                                                                       a, bp, list, nbig);
                 OSTEP("orbit_process_big");
                 ctx->prof.kernel_launches++;
             }
-            CK(cudaGetLastError());
             u32 hr = 0;
             CK(cudaMemcpyAsync(ctx->h_oc, ctx->d_oc, sizeof(OrbitCounters), cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaMemcpyAsync(&hr, nretry, 4, cudaMemcpyDeviceToHost, ctx->stream));
@@ -797,7 +812,8 @@ struct Engine {
             if (hr == 0) return 0;
             std::swap(list, other);
             nbig = hr;
-            rcap *= 4;
+            if (!smem_pass) rcap *= 4;
+            smem_pass = false;
             if (rcap > (1ull << 26)) return set_err(ctx, FFG_ERR_STATE, "orbit group larger than 2^26 terms");
         }
         return 0;
@@ -860,6 +876,7 @@ struct Engine {
         a.thr = t ? t->thr : 0;
         a.tau = t ? t->tau : 0.0;
         a.max_xweight = t ? t->max_xweight : -1;
+        a.route_big = ctx->orbit_route_big;
         u64 out_cap = std::max<u64>(cap, pow2_at_least(4 * n_in));
         constexpr int NWo = PAULI ? NW : 1;
         const size_t smem = sizeof(OrbitTable<KW, CPLX>) * kOrbitWarps;
@@ -919,6 +936,14 @@ struct Engine {
             ctx->prof.orbit_max_group = std::max<int64_t>(ctx->prof.orbit_max_group, oc.max_members);
             ctx->prof.orbit_batches++;
             ctx->prof.orbit_groups += oc.ngroups;
+            if (getenv("FFG_ORBIT_STATS")) {
+                fprintf(stderr, "batch k=%d n_in=%llu groups=%u big=%u wasted=%u out=%llu |", k,
+                        (unsigned long long)n_in, oc.ngroups, oc.nbig, oc.wasted, (unsigned long long)oc.n_out);
+                for (int b = 0; b < 16; b++) fprintf(stderr, " %u", oc.hist[b]);
+                fprintf(stderr, " | A:");
+                for (int b = 0; b < 16; b++) fprintf(stderr, " %u", oc.hist_a[b]);
+                fprintf(stderr, "\n");
+            }
             // the output store becomes the live store
             cur = dst;
             cap = out_cap;
@@ -1294,6 +1319,7 @@ int ffg_create(ffg_ctx** out, int device) {
     if (const char* d = getenv("FFG_PERSIST_BPS")) ctx->persist_blocks_per_sm = std::max(1, atoi(d));
     if (const char* d = getenv("FFG_ORBIT")) ctx->orbit = atoi(d) != 0;
     if (const char* d = getenv("FFG_ORBIT_MIN")) ctx->orbit_min_gates = std::max(1, atoi(d));
+    if (const char* d = getenv("FFG_ORBIT_ROUTE")) ctx->orbit_route_big = std::max(1, atoi(d));
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);

@@ -70,6 +70,9 @@ struct OrbitCounters {
     u32 big_overflow;  // a block-level group outgrew its region
     u32 chk_code;      // self-check builds: first failed check (0 = none)
     u32 chk_a, chk_b, chk_c;
+    u32 hist[16];      // completed groups by floor(log2(final members))
+    u32 hist_a[16];    // completed groups by |A| (capped at 15)
+    u32 wasted;        // groups abandoned by the warp pass after growing past its table
 };
 
 #ifdef FFG_ORBIT_CHECK
@@ -94,6 +97,7 @@ struct OrbitBatchArgs {
     int thr;
     double tau;
     int max_xweight;
+    int route_big;  // groups with at least this many gates in A go straight to the block-level pass
 };
 
 template <int NW, bool CPLX>
@@ -345,7 +349,10 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
         OCHK(rep < sc.cap_in, 14, rep, g, ng)
         const u32 m0 = sc.cnt[rep];
         const u32 base = sc.off[rep];
-        if (m0 > kOrbitCap) {
+        int na = 0;
+#pragma unroll
+        for (int w = 0; w < kAW; w++) na += __popcll(sc.amask[(u64)w * sc.cap_in + rep]);
+        if (m0 > kOrbitCap || na >= a.route_big) {
             if (lane == 0) {
                 sc.big[atomicAdd(&oc->nbig, 1u)] = rep;
                 atomicMax(&oc->max_members, m0);
@@ -450,7 +457,10 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
         }
         __syncwarp();
         if (*(volatile unsigned int*)&T.flag) {
-            if (lane == 0) sc.big[atomicAdd(&oc->nbig, 1u)] = rep;
+            if (lane == 0) {
+                sc.big[atomicAdd(&oc->nbig, 1u)] = rep;
+                atomicAdd(&oc->wasted, 1u);
+            }
             continue;
         }
         emits += g_emits;
@@ -458,7 +468,13 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
         xapps += g_xapps;
         // survivors of the batch-end truncation go to the output store
         const int cnt = (int)*(volatile unsigned int*)&T.cnt;
-        if (lane == 0) atomicMax(&oc->max_members, (u32)cnt);
+        if (lane == 0) {
+            atomicMax(&oc->max_members, (u32)cnt);
+            atomicAdd(&oc->hist[31 - __clz(cnt | 1)], 1u);
+            int na = 0;
+            for (int w = 0; w < kAW; w++) na += __popcll(A[w]);
+            atomicAdd(&oc->hist_a[na < 15 ? na : 15], 1u);
+        }
         for (int m = lane; m < cnt; m += 32) {
             const cplx c = {T.re[m], CPLX ? T.im[m] : 0.0};
             if (survives<NW, CPLX>(T.key[m], c, a)) out_append<KW, CPLX>(out, oc, T.key[m], c);
@@ -514,19 +530,27 @@ __device__ __forceinline__ BigRegion<KW, CPLX> big_region(const BigPool& bp, u32
     return g;
 }
 
-template <int KW, bool CPLX>
+// loads from a block-level table: L2 for global-memory regions, volatile for
+// shared memory
+template <bool SM, typename T>
+__device__ __forceinline__ T tld(const T* p) {
+    if (SM) return *(const volatile T*)p;
+    return __ldcg(p);
+}
+
+template <int KW, bool CPLX, bool SM = false>
 __device__ __forceinline__ int big_find(const BigRegion<KW, CPLX>& G, u32 rcap, const u64* k) {
     const u32 mask = 2 * rcap - 1;
     u32 pos = small_hash<KW>(k) & mask;
     for (u32 probe = 0; probe <= mask; probe++) {
-        const u32 m = __ldcg(&G.slot[pos]);
+        const u32 m = tld<SM>(&G.slot[pos]);
         if (m == 0xffffffffu) return -1;
 #ifdef FFG_ORBIT_CHECK
         if (m >= rcap) return (int)0x7fffffff;
 #endif
         bool eq = true;
 #pragma unroll
-        for (int w = 0; w < KW; w++) eq = eq && __ldcg(&G.key[(u64)w * rcap + m]) == k[w];
+        for (int w = 0; w < KW; w++) eq = eq && tld<SM>(&G.key[(u64)w * rcap + m]) == k[w];
         if (eq) return (int)m;
         pos = (pos + 1) & mask;
     }
@@ -543,19 +567,46 @@ __device__ __forceinline__ void big_insert(const BigRegion<KW, CPLX>& G, u32 rca
     }
 }
 
-template <int NW, bool CPLX>
+constexpr u32 kBlockCap = 4096;  // members of a block-level table held in shared memory
+
+template <int KW, bool CPLX>
+constexpr size_t block_table_bytes() {
+    return (size_t)KW * kBlockCap * 8 + kBlockCap * 8 * (CPLX ? 2 : 1) + 2 * kBlockCap * 4 + 16;
+}
+
+// Block-level group processing.  SM: the table lives in dynamic shared memory
+// (kBlockCap members); otherwise in the block's global-memory region of bp.
+template <int NW, bool CPLX, bool SM>
 __global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreView out, OrbitScratch sc,
                                                           OrbitCounters* oc, OrbitBatchArgs a, BigPool bp,
                                                           const u32* list, u32 nlist) {
     constexpr int KW = 2 * NW;
     __shared__ long long red[3][32];
+    extern __shared__ __align__(16) unsigned char btab[];
     long long emits = 0, created = 0, xapps = 0;
     for (u32 gi = blockIdx.x; gi < nlist; gi += gridDim.x) {
         OCHK(gi < sc.cap_in, 8, gi, nlist, 0)
         const u32 rep = list[gi];
         OCHK(rep < sc.cap_in, 9, rep, gi, nlist)
-        const BigRegion<KW, CPLX> G = big_region<KW, CPLX>(bp, blockIdx.x);
-        const u32 rcap = bp.rcap;
+        BigRegion<KW, CPLX> G;
+        u32 rcap;
+        if (SM) {
+            rcap = kBlockCap;
+            char* p = (char*)btab;
+            G.key = (u64*)p;
+            p += (size_t)KW * kBlockCap * 8;
+            G.re = (double*)p;
+            p += kBlockCap * 8;
+            G.im = (double*)p;
+            if (CPLX) p += kBlockCap * 8;
+            G.slot = (u32*)p;
+            p += 2 * kBlockCap * 4;
+            G.cnt = (u32*)p;
+            G.flag = G.cnt + 1;
+        } else {
+            G = big_region<KW, CPLX>(bp, blockIdx.x);
+            rcap = bp.rcap;
+        }
         const u32 m0 = sc.cnt[rep];
         const u32 base = sc.off[rep];
         for (u32 s2 = threadIdx.x; s2 < 2 * rcap; s2 += blockDim.x) G.slot[s2] = 0xffffffffu;
@@ -606,7 +657,7 @@ __global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreVie
                     u64 q[KW], k[KW];
 #pragma unroll
                     for (int w = 0; w < KW; w++) {
-                        q[w] = __ldcg(&G.key[(u64)w * rcap + m]);
+                        q[w] = tld<SM>(&G.key[(u64)w * rcap + m]);
                         k[w] = q[w] ^ P[w];
                     }
                     int yQ = 0, yK = 0, zxQ = 0, zxK = 0, dQ = 0, dK = 0;
@@ -621,12 +672,12 @@ __global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreVie
                     }
                     const int jQ = Gt.yP + yQ + 2 * zxQ - yK;
                     const int jK = Gt.yP + yK + 2 * zxK - yQ;
-                    const cplx ci = {__ldcg(&G.re[m]), CPLX ? __ldcg(&G.im[m]) : 0.0};
-                    const int j = big_find<KW, CPLX>(G, rcap, k);
+                    const cplx ci = {tld<SM>(&G.re[m]), CPLX ? tld<SM>(&G.im[m]) : 0.0};
+                    const int j = big_find<KW, CPLX, SM>(G, rcap, k);
                     OCHK(j < (int)rcap, 6, j, rcap, m)
                     if (j >= 0 && (u32)j < cnt0) {
                         if ((u32)j < m) continue;
-                        const cplx cj = {__ldcg(&G.re[j]), CPLX ? __ldcg(&G.im[j]) : 0.0};
+                        const cplx cj = {tld<SM>(&G.re[j]), CPLX ? tld<SM>(&G.im[j]) : 0.0};
                         cplx ni = cscale(ci, Gt.c), nj = cscale(cj, Gt.c);
                         if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
                         if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
@@ -674,13 +725,19 @@ __global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreVie
         created += g_created;
         xapps += g_xapps;
         const u32 cnt = *(volatile u32*)G.cnt;
-        if (threadIdx.x == 0) atomicMax(&oc->max_members, cnt);
+        if (threadIdx.x == 0) {
+            atomicMax(&oc->max_members, cnt);
+            atomicAdd(&oc->hist[31 - __clz(cnt | 1)], 1u);
+            int na = 0;
+            for (int w = 0; w < kAW; w++) na += __popcll(sc.amask[(u64)w * sc.cap_in + rep]);
+            atomicAdd(&oc->hist_a[na < 15 ? na : 15], 1u);
+        }
         for (u32 m = threadIdx.x; m < cnt; m += blockDim.x) {
             OCHK(m < rcap, 7, m, cnt, rcap)
             u64 k[KW];
 #pragma unroll
-            for (int w = 0; w < KW; w++) k[w] = __ldcg(&G.key[(u64)w * rcap + m]);
-            const cplx c = {__ldcg(&G.re[m]), CPLX ? __ldcg(&G.im[m]) : 0.0};
+            for (int w = 0; w < KW; w++) k[w] = tld<SM>(&G.key[(u64)w * rcap + m]);
+            const cplx c = {tld<SM>(&G.re[m]), CPLX ? tld<SM>(&G.im[m]) : 0.0};
             if (survives<NW, CPLX>(k, c, a)) out_append<KW, CPLX>(out, oc, k, c);
         }
         __syncthreads();
