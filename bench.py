@@ -334,8 +334,10 @@ def main():
                        "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas{ws}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": None,
-                         "kernel": "pauli_rot_kernel<2,false>",
-                         "algorithmic_bytes": "40 B x (2 x apps + emitted partners) per rotation pass",
+                         "kernel": "orbit engine (orbit_classify..orbit_process_big) + persistent per-gate kernel",
+                         "launch_unit": "one commuting run (orbit batch) or one persistent run",
+                         "algorithmic_bytes": "40 B x (2 x apps + emitted partners): per-gate model, "
+                                              "summed over the gates of each launch",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // n_e2e,
