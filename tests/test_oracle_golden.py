@@ -11,7 +11,7 @@ import pytest
 from golden_io import assert_same_terms, checksum, fixture_names, load
 from oracle import oracle as O
 
-SLOW = {n for n in fixture_names() if float(load(n)["ref_seconds"]) > 2.0}
+SLOW = {n for n in fixture_names() if float(load(n)["ref_seconds"]) > 30.0}
 
 
 def run_oracle(fx, n_threads=1):
