@@ -8,6 +8,11 @@ One step = the whole theta_h sweep (7 propagations).  Term-gate applications
 ("apps") = sum over rotation gates of the live terms entering the gate.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload kicked_ising|hubbard]
+
+--workload hubbard measures the 6x6 Fermi-Hubbard Majorana propagation (144
+Majoranas, 10 Trotter steps, degree <= 6, tau = 1e-7) instead; one step = one
+propagation.
 
 Prints one JSON line on rank 0.  Multi-GPU runs are independent replicas (the
 propagation of one observable does not shard without a per-gate exchange):
@@ -27,13 +32,110 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "term-gate applications/s (10x10 kicked Ising, 20 steps, W=8, tau=1e-6, theta_h sweep)"
 UNIT = "apps/s"
-THETAS = (0.1, 0.3, 0.5, 0.7, 0.9, 1.1, math.pi / 2)
 MAXDEG, TAU = 8, 1e-6
 OBS_SITE = 55
-BYTES_PER_TERM = 32 + 8   # 128-bit x and z masks + FP64 coefficient (real mode)
-CPU_SAMPLE_THETAS = (0.1, 0.9)
+
+
+class KickedIsing:
+    """10x10 kicked Ising (the headline workload); one step = the theta_h sweep."""
+    name = "kicked_ising_10x10_w8_tau1e-6"
+    metric = "term-gate applications/s (10x10 kicked Ising, 20 steps, W=8, tau=1e-6, theta_h sweep)"
+    kind = "pauli"
+    bytes_per_term = 32 + 8  # 128-bit x and z masks + FP64 coefficient (real mode)
+    kernel = "orbit engine (orbit_classify..orbit_process_big) + persistent per-gate kernel"
+    launch_unit = "one commuting run (orbit batch) or one persistent run"
+    thetas = (0.1, 0.3, 0.5, 0.7, 0.9, 1.1, math.pi / 2)
+    cpu_thetas = (0.1, 0.9)
+    params = dict(maxdegree=MAXDEG, topk=0, mincoeff=TAU, max_xweight=-1, xtrunc_period=1,
+                  batched=1, deterministic=0)
+
+    def tables(self):
+        import fastfermion_gb300 as ff
+        return [ff.encode_pauli_circuit(ff.build_circuit(ff.workloads.kicked_ising_circuit(th)))
+                for th in self.thetas]
+
+    def observable(self):
+        keys = np.zeros((4, 1), dtype=np.uint64)
+        keys[2, 0] = np.uint64(1) << np.uint64(OBS_SITE)
+        return keys, np.ones(1), np.zeros(1)
+
+    def propagate(self, ctx, k, re, im, tab, n=None):
+        p = dict(self.params)
+        if n is not None:
+            p["n"] = n
+        return ctx.pauli_propagate(k, re, im, tab, p, on_device=n is not None)
+
+    def cpu_sample(self, tabs, cores):
+        """The oracle's sharded OpenMP port of the reference on a subset of theta_h."""
+        from oracle import oracle as O
+        keys, re, im = self.observable()
+        apps = 0
+        t0 = time.perf_counter()
+        for th, tab in zip(self.thetas, tabs):
+            if th in self.cpu_thetas:
+                apps += O.pauli_propagate(tab, keys, re, im, maxdegree=MAXDEG, mincoeff=TAU,
+                                          n_threads=cores).apps
+        return apps, time.perf_counter() - t0, cores, (
+            f"theta_h in {list(self.cpu_thetas)} of the same workload, sharded OpenMP port "
+            "of the reference algorithm")
+
+    def config(self):
+        return {"workload": self.name, "lattice": "10x10 open", "trotter_steps": 20,
+                "maxdegree": MAXDEG, "mincoeff": TAU, "theta_h": [round(t, 6) for t in self.thetas],
+                "observable": "Z_55", "batched": True}
+
+
+class Hubbard:
+    """6x6 spinful Fermi-Hubbard in Majorana form (144 Majoranas), 10 Trotter steps,
+    t=1, U=4, dt=0.1, observable n_(0,up) = 0.5 (1 + i g0 g1), degree <= 6, tau = 1e-7."""
+    name = "hubbard_6x6_10steps_deg6_tau1e-7"
+    metric = "term-gate applications/s (6x6 Fermi-Hubbard Majorana, 10 steps, deg<=6, tau=1e-7)"
+    kind = "majorana"
+    bytes_per_term = 24 + 16  # 3 words of Majorana bits + complex FP64 coefficient
+    kernel = "persistent per-gate kernel (pass_mrot, threshold after every gate)"
+    launch_unit = "one persistent run"
+    steps = 10
+    cpu_steps = 6
+    params = dict(has_maxdegree=1, maxdegree=6, mincoeff=1e-7, deterministic=0)
+
+    def _table(self, steps):
+        import fastfermion_gb300 as ff
+        return ff.encode_majorana_circuit(ff.build_circuit(ff.workloads.hubbard_circuit(6, 6, steps=steps)))
+
+    def tables(self):
+        return [self._table(self.steps)]
+
+    def observable(self):
+        keys = np.zeros((4, 2), dtype=np.uint64)
+        keys[0, 1] = 3  # g0 g1
+        return keys, np.array([0.5, 0.0]), np.array([0.0, 0.5])
+
+    def propagate(self, ctx, k, re, im, tab, n=None):
+        p = dict(self.params)
+        if n is not None:
+            p["n"] = n
+        return ctx.majorana_propagate(k, re, im, tab, p, on_device=n is not None)
+
+    def cpu_sample(self, tabs, cores):
+        """The oracle's serial port (the reference's Majorana path is serial) on the
+        first cpu_steps Trotter steps."""
+        from oracle import oracle as O
+        keys, re, im = self.observable()
+        tab = self._table(self.cpu_steps)
+        t0 = time.perf_counter()
+        r = O.majorana_propagate(tab, keys, re, im, maxdegree=6, mincoeff=1e-7)
+        return r.apps, time.perf_counter() - t0, 1, (
+            f"the first {self.cpu_steps} of 10 Trotter steps, serial port of the reference "
+            "algorithm (the reference's Majorana path has no parallel strategy)")
+
+    def config(self):
+        return {"workload": self.name, "lattice": "6x6 open, spinful (144 Majoranas)",
+                "trotter_steps": self.steps, "t": 1.0, "U": 4.0, "dt": 0.1, "maxdegree": 6,
+                "mincoeff": 1e-7, "observable": "0.5 (1 + i g0 g1)"}
+
+
+WORKLOADS = {"kicked_ising": KickedIsing, "hubbard": Hubbard}
 
 
 def parse():
@@ -42,32 +144,17 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="kicked_ising", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-roofline", action="store_true")
     ap.add_argument("--thetas", default=None,
                     help="comma-separated subset of theta_h (profiling runs; not a bench line)")
     a = ap.parse_args()
+    a.wl = WORKLOADS[a.workload]()
     if a.thetas:
-        global THETAS
-        THETAS = tuple(float(t) for t in a.thetas.split(","))
+        a.wl.thetas = tuple(float(t) for t in a.thetas.split(","))
     return a
-
-
-def tables():
-    import fastfermion_gb300 as ff
-    return [ff.encode_pauli_circuit(ff.build_circuit(ff.workloads.kicked_ising_circuit(th)))
-            for th in THETAS]
-
-
-def observable():
-    keys = np.zeros((4, 1), dtype=np.uint64)
-    keys[2, 0] = np.uint64(1) << np.uint64(OBS_SITE)
-    return keys, np.ones(1), np.zeros(1)
-
-
-PARAMS = dict(maxdegree=MAXDEG, topk=0, mincoeff=TAU, max_xweight=-1, xtrunc_period=1, batched=1,
-              deterministic=0)
 
 
 # ---------------------------------------------------------------------------
@@ -168,23 +255,12 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline (the oracle's sharded OpenMP port of the reference algorithm)
+# CPU baseline (the oracle's port of the reference algorithm)
 # ---------------------------------------------------------------------------
-def cpu_baseline(tabs):
-    from oracle import oracle as O
-    keys, re, im = observable()
-    cores = os.cpu_count() or 1
-    apps = 0
-    t0 = time.perf_counter()
-    for th, tab in zip(THETAS, tabs):
-        if th not in CPU_SAMPLE_THETAS:
-            continue
-        r = O.pauli_propagate(tab, keys, re, im, maxdegree=MAXDEG, mincoeff=TAU, n_threads=cores)
-        apps += r.apps
-    dt = time.perf_counter() - t0
+def cpu_baseline(wl, tabs):
+    apps, dt, cores, desc = wl.cpu_sample(tabs, os.cpu_count() or 1)
     return {"value": apps / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"theta_h in {list(CPU_SAMPLE_THETAS)} of the same workload ({apps} apps, "
-                      f"{dt:.1f} s, sharded OpenMP port of the reference algorithm)"}
+            "sample": f"{desc} ({apps} apps, {dt:.1f} s)"}
 
 
 def run_reference(args):
@@ -193,33 +269,23 @@ def run_reference(args):
         return 0
     from oracle import oracle as O
     O.build()
-    tabs = tables()
-    keys, re, im = observable()
-    cores = os.cpu_count() or 1
-
-    def step():
-        apps = 0
-        for th, tab in zip(THETAS, tabs):
-            if th in CPU_SAMPLE_THETAS:
-                apps += O.pauli_propagate(tab, keys, re, im, maxdegree=MAXDEG, mincoeff=TAU,
-                                          n_threads=cores).apps
-        return apps
-
+    wl = args.wl
+    tabs = wl.tables()
     for _ in range(args.warmup):
-        step()
-    tot, t0 = 0, time.perf_counter()
+        wl.cpu_sample(tabs, os.cpu_count() or 1)
+    tot, dt = 0, 0.0
     for _ in range(args.steps):
-        tot += step()
-    dt = time.perf_counter() - t0
+        apps, t, cores, desc = wl.cpu_sample(tabs, os.cpu_count() or 1)
+        tot += apps
+        dt += t
     v = tot / dt
     print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "impl": "reference", "metric": wl.metric, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": "kicked_ising_10x10_w8_tau1e-6",
-                                        "sample_thetas": list(CPU_SAMPLE_THETAS)},
+        "data": "synthetic", "config": wl.config(),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"theta_h in {list(CPU_SAMPLE_THETAS)} per step"},
+                         "sample": f"{desc}, per step"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
     return 0
 
@@ -239,8 +305,9 @@ def main():
     torch.cuda.set_device(local)
     ctx = _native.context(local)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
-    tabs = tables()
-    hk, hre, him = observable()
+    wl = args.wl
+    tabs = wl.tables()
+    hk, hre, him = wl.observable()
     dk = torch.from_numpy(hk.astype(np.int64)).cuda()
     dre = torch.from_numpy(hre).cuda()
     dim = torch.from_numpy(him).cuda()
@@ -251,10 +318,7 @@ def main():
         ctx.set_profiling(profiling)
         apps, emits, launches, rot_s, nrot = 0, 0, 0, 0.0, 0
         for tab in tabs:
-            p = dict(PARAMS)
-            p["n"] = 1
-            r = ctx.pauli_propagate(dk.data_ptr(), dre.data_ptr(), dim.data_ptr(), tab, p,
-                                    on_device=True)
+            r = wl.propagate(ctx, dk.data_ptr(), dre.data_ptr(), dim.data_ptr(), tab, n=hre.size)
             pr = ctx.profile()
             apps += pr["apps"]
             emits += pr["emits"]
@@ -293,7 +357,7 @@ def main():
     achieved = None
     if not args.no_roofline:
         a_p, e_p, _, rot_s, nrot = step_device(profiling=True)
-        alg_bytes = BYTES_PER_TERM * (2 * a_p + e_p)
+        alg_bytes = wl.bytes_per_term * (2 * a_p + e_p)
         achieved = alg_bytes / rot_s / 1e9 if rot_s > 0 else None
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -307,9 +371,9 @@ def main():
     for _ in range(0 if args.no_e2e else max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
         for tab in tabs:
-            r = ctx.pauli_propagate(hk, hre, him, tab, dict(PARAMS))
+            r = wl.propagate(ctx, hk, hre, him, tab)
             keys, re, im = r.copy()
-            r.overlapwithzero()
+            r.overlapwithzero() if wl.kind == "pauli" else r.fock_state(0, 0)
             d2h += keys.nbytes + re.nbytes + im.nbytes
             h2d += hk.nbytes + hre.nbytes + him.nbytes + tab.nbytes
             r.free()
@@ -320,24 +384,20 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(tabs)
+        cpu = cpu_baseline(wl, tabs)
 
     if rank == 0:
         out = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "metric": wl.metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "kicked_ising_10x10_w8_tau1e-6", "lattice": "10x10 open",
-                       "trotter_steps": 20, "maxdegree": MAXDEG, "mincoeff": TAU,
-                       "theta_h": [round(t, 6) for t in THETAS], "observable": "Z_55",
-                       "batched": True, "apps_per_step": apps_tot / args.steps,
-                       "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas{ws}"},
+            "config": dict(wl.config(), apps_per_step=apps_tot / args.steps,
+                           l2="flushed between steps (512 MB write)", parallelism=f"replicas{ws}"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": None,
-                         "kernel": "orbit engine (orbit_classify..orbit_process_big) + persistent per-gate kernel",
-                         "launch_unit": "one commuting run (orbit batch) or one persistent run",
-                         "algorithmic_bytes": "40 B x (2 x apps + emitted partners): per-gate model, "
-                                              "summed over the gates of each launch",
+                         "kernel": wl.kernel, "launch_unit": wl.launch_unit,
+                         "algorithmic_bytes": f"{wl.bytes_per_term} B x (2 x apps + emitted partners): "
+                                              "per-gate model, summed over the gates of each launch",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // n_e2e,

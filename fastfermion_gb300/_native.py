@@ -154,15 +154,21 @@ class Context:
                                               ctypes.byref(out)))
         return Result(self, out)
 
-    def majorana_propagate(self, keys, re, im, gates, params):
+    def majorana_propagate(self, keys, re, im, gates, params, on_device=False):
+        """keys: uint64 (4, n); re, im: float64 (n,); gates: MAJORANA_GATE array.
+        With on_device, keys/re/im are integer device addresses instead."""
         out = ctypes.c_void_p()
-        keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
-        re = np.ascontiguousarray(re, dtype=np.float64)
-        im = None if im is None else np.ascontiguousarray(im, dtype=np.float64)
+        if on_device:
+            kp, rp, ip, n = keys, re, im, params.pop("n")
+        else:
+            keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
+            re = np.ascontiguousarray(re, dtype=np.float64)
+            im = None if im is None else np.ascontiguousarray(im, dtype=np.float64)
+            kp, rp, ip, n = _ptr(keys), _ptr(re), _ptr(im), re.size
         gates = np.ascontiguousarray(gates, dtype=MAJORANA_GATE)
         p = MajoranaParams(**params)
-        self.check(self.L.ffg_majorana_propagate(self.h, _ptr(keys), _ptr(re), _ptr(im), re.size,
-                                                 _ptr(gates), gates.size, ctypes.byref(p), 0,
+        self.check(self.L.ffg_majorana_propagate(self.h, kp, rp, ip, n, _ptr(gates), gates.size,
+                                                 ctypes.byref(p), int(bool(on_device)),
                                                  ctypes.byref(out)))
         return Result(self, out)
 

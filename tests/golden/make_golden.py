@@ -354,6 +354,8 @@ def cases(ff):
     yield "hubbard_3x3", lambda: hub("hubbard_3x3", 3, 3, 10, 6, 1e-7)
     yield "hubbard_6x6_2steps", lambda: hub("hubbard_6x6_2steps", 6, 6, 2, 6, 1e-7)
     yield "hubbard_6x6_3steps", lambda: hub("hubbard_6x6_3steps", 6, 6, 3, 6, 1e-7)
+    # the full 6x6 Hubbard workload: 10 steps, ~1.2e7 final terms, minutes on the reference
+    yield "hubbard_6x6_10steps", lambda: hub("hubbard_6x6_10steps", 6, 6, 10, 6, 1e-7)
 
 
 REF = "/root/reference"
