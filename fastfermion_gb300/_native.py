@@ -31,6 +31,11 @@ class MajoranaParams(ctypes.Structure):
                 ("pad", ctypes.c_int32)]
 
 
+class BatchParams(ctypes.Structure):
+    _fields_ = [("ninst", ctypes.c_size_t), ("offsets", ctypes.c_void_p), ("thetas", ctypes.c_void_p),
+                ("checkpoint_every", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
 class Profile(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in (
         "seconds_total", "seconds_rotations", "seconds_truncate", "seconds_clifford",
@@ -50,7 +55,9 @@ EXPORTS = ["ffg_create", "ffg_destroy", "ffg_last_error", "ffg_set_profiling", "
            "ffg_pauli_propagate", "ffg_majorana_propagate", "ffg_result_size", "ffg_result_kind",
            "ffg_result_copy", "ffg_result_device", "ffg_result_overlapwithzero",
            "ffg_result_qubit_state", "ffg_result_fock_state", "ffg_result_free", "ffg_abs_le",
-           "ffg_pauli_schedule", "ffg_stream", "ffg_pauli_rotations_noalloc"]
+           "ffg_pauli_schedule", "ffg_stream", "ffg_pauli_rotations_noalloc",
+           "ffg_pauli_propagate_batched", "ffg_batch_size", "ffg_batch_copy", "ffg_batch_adjoint",
+           "ffg_batch_free"]
 
 
 def lib():
@@ -90,6 +97,13 @@ def lib():
             L.ffg_pauli_rotations_noalloc.argtypes = [vp, vp, vp, vp, sz, vp, sz, ctypes.c_int32,
                                                       vp, vp, vp, sz, ctypes.POINTER(sz),
                                                       ctypes.c_char_p, sz]
+            L.ffg_pauli_propagate_batched.argtypes = [vp, vp, vp, sz, vp, sz, ctypes.POINTER(PauliParams),
+                                                      ctypes.POINTER(BatchParams), vp, ctypes.POINTER(vp)]
+            L.ffg_batch_size.restype = sz
+            L.ffg_batch_size.argtypes = [vp]
+            L.ffg_batch_copy.argtypes = [vp, vp, vp, vp]
+            L.ffg_batch_adjoint.argtypes = [vp, vp, vp, vp]
+            L.ffg_batch_free.argtypes = [vp]
             L.ffg_pauli_schedule.restype = i64
             L.ffg_pauli_schedule.argtypes = [vp, sz, ctypes.c_int, vp, i64]
             _lib = L
@@ -172,10 +186,66 @@ class Context:
                                                  ctypes.byref(out)))
         return Result(self, out)
 
+    def pauli_propagate_batched(self, keys, re, offsets, gates, thetas, params, checkpoint_every=1):
+        """Batched propagation (ffg_pauli_propagate_batched).  keys: uint64 (4, n) of all
+        instances, re: float64 (n,), offsets: int64 (ninst+1,), thetas: float64
+        (ninst, nrot) or None.  Returns (expect[ninst], Batch or None)."""
+        keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
+        re = np.ascontiguousarray(re, dtype=np.float64)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        gates = np.ascontiguousarray(gates, dtype=PAULI_GATE)
+        ninst = offsets.size - 1
+        th = None if thetas is None else np.ascontiguousarray(thetas, dtype=np.float64)
+        bp = BatchParams(ninst, offsets.ctypes.data, th.ctypes.data if th is not None and th.size else None,
+                         int(checkpoint_every), 0)
+        p = PauliParams(**params)
+        expect = np.zeros(ninst)
+        out = ctypes.c_void_p()
+        self.check(self.L.ffg_pauli_propagate_batched(self.h, _ptr(keys), _ptr(re), re.size, _ptr(gates),
+                                                      gates.size, ctypes.byref(p), ctypes.byref(bp),
+                                                      _ptr(expect), ctypes.byref(out)))
+        return expect, Batch(self, out, ninst, int(np.sum(gates["kind"] == ROT)), re.size)
+
     def __del__(self):
         if getattr(self, "h", None) and self.h.value:
             self.L.ffg_destroy(self.h)
             self.h = ctypes.c_void_p()
+
+
+class Batch:
+    """Handle of a batched propagation: final term sets and the adjoint."""
+
+    def __init__(self, ctx, handle, ninst, nrot, n_input):
+        self.ctx, self.h, self.ninst, self.nrot, self.n_input = ctx, handle, ninst, nrot, n_input
+        self.n = ctx.L.ffg_batch_size(handle)
+
+    def copy(self):
+        """(keys (4, n) without instance bits, re (n,), inst (n,))"""
+        keys = np.zeros((4, self.n), dtype=np.uint64)
+        re = np.zeros(self.n)
+        inst = np.zeros(self.n, dtype=np.int64)
+        if self.n:
+            self.ctx.check(self.ctx.L.ffg_batch_copy(self.h, _ptr(keys), _ptr(re), _ptr(inst)))
+        return keys, re, inst
+
+    def adjoint(self, weights, with_coef=False):
+        """(grad_theta (ninst, nrot), grad_coef (n_input,) or None) of sum_i w_i <O_i>."""
+        w = np.ascontiguousarray(weights, dtype=np.float64).reshape(self.ninst)
+        g = np.zeros((self.ninst, self.nrot))
+        gc = np.zeros(self.n_input) if with_coef else None
+        self.ctx.check(self.ctx.L.ffg_batch_adjoint(self.h, _ptr(w), _ptr(g), _ptr(gc) if with_coef else None))
+        return g, gc
+
+    def free(self):
+        if self.h is not None and self.h.value:
+            self.ctx.L.ffg_batch_free(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 class Result:

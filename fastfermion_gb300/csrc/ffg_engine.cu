@@ -24,6 +24,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -31,6 +32,7 @@
 #include "ffg_kernels.cuh"
 #include "ffg_persist.cuh"
 #include "ffg_orbit.cuh"
+#include "ffg_adjoint.cuh"
 
 using namespace ffg;
 
@@ -113,6 +115,29 @@ struct PendingEvent {
     int phase;
 };
 
+// One step of a batched propagation, kept for the adjoint: a range of Clifford
+// ops run by the persistent kernel, or one orbit batch.
+struct AdjRecord {
+    enum Type { CLIFF, ORBIT } type;
+    size_t op_begin = 0, op_end = 0;  // CLIFF: ops [op_begin, op_end)
+    int g0 = 0, k = 0;                // ORBIT: batch gates [g0, g0 + k)
+    bool has_trunc = false;
+    TruncArgs trunc{};
+    u64 n_in = 0;                     // terms entering the step
+    u64* key = nullptr;               // checkpoint of the terms entering the step:
+    double* re = nullptr;             //   KW planes of n_in keys (stride n_in) + coefficients
+    bool temp = false;                // recomputed during the backward pass
+};
+
+// Instance layout of a batched propagation (see ffg_adjoint.cuh).
+struct BatchCtx {
+    const double2* d_inst_cs = nullptr;  // [batch gates][ninst] (cos, sin)
+    u32 ninst = 0;
+    int inst_plane = 0;                  // store plane of the instance code
+    int inst_shift = 0;
+    u64 inst_mask = 0;
+};
+
 }  // namespace
 
 struct ffg_ctx {
@@ -154,6 +179,7 @@ struct ffg_ctx {
     OrbitCounters* d_oc = nullptr;
     OrbitCounters* h_oc = nullptr;  // pinned
     RawBuf bigpool;                 // global-memory tables of large orbit groups
+    const BatchCtx* batch = nullptr;  // set while a batched propagation runs
     ffg_profile prof{};
     std::vector<PendingEvent> events;
     std::vector<cudaEvent_t> free_events;
@@ -171,6 +197,30 @@ struct ffg_result {
     double* im = nullptr;
     unsigned char* dead = nullptr;  // zeros (lets the reduction kernels share the store view)
     ffg_ctx* ctx = nullptr;
+};
+
+// A batched propagation: the final term set, the schedule and the checkpoints
+// the adjoint needs.  Device memory here belongs to the handle.
+struct ffg_batch {
+    ffg_ctx* ctx = nullptr;
+    int kw = 2;                      // key planes (2: qubits and instance bits below 64; 4 otherwise)
+    size_t ninst = 0, nrot = 0, n_input = 0;
+    BatchCtx bc{};
+    double2* d_inst_cs = nullptr;
+    u64 xmask[2] = {0, 0};           // qubit bits of the x planes (caller words 0, 1)
+    int inst_word = 0;               // caller word that holds the instance code
+    int maxdeg = 128;                // degree filter including the instance bits
+    std::vector<ffg_pauli_gate> gates;
+    std::vector<Op> ops;
+    std::vector<RotArgs> rots;
+    std::vector<TruncArgs> truncs;
+    std::vector<GArgs> groups;
+    std::vector<BatchInfo> binfo;
+    std::vector<AdjRecord> recs;
+    int every = 0;                   // checkpoint every `every` steps (0: none)
+    u64* fkey = nullptr;             // final term set: kw planes, stride fn
+    double* fre = nullptr;
+    u64 fn = 0;
 };
 
 namespace {
@@ -877,6 +927,13 @@ struct Engine {
         a.tau = t ? t->tau : 0.0;
         a.max_xweight = t ? t->max_xweight : -1;
         a.route_big = ctx->orbit_route_big;
+        if (ctx->batch) {
+            a.inst_cs = ctx->batch->d_inst_cs + (size_t)g0 * ctx->batch->ninst;
+            a.ninst = ctx->batch->ninst;
+            a.inst_plane = ctx->batch->inst_plane;
+            a.inst_shift = ctx->batch->inst_shift;
+            a.inst_mask = ctx->batch->inst_mask;
+        }
         u64 out_cap = std::max<u64>(cap, pow2_at_least(4 * n_in));
         constexpr int NWo = PAULI ? NW : 1;
         const size_t smem = sizeof(OrbitTable<KW, CPLX>) * kOrbitWarps;
@@ -963,16 +1020,12 @@ struct Engine {
         return set_err(ctx, FFG_ERR_STATE, "orbit batch: output store kept overflowing");
     }
 
-    // Pauli batched runs: long commuting runs go through the batch-orbit path,
-    // everything else through persistent per-gate runs.
-    int run_mixed(const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
-                  const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups,
-                  const std::vector<BatchInfo>& batches, int maxdeg) {
-        int rc = prepare_persistent(ops, rots, truncs, groups);
-        if (rc) return rc;
-        // batch gate table, in op order
+    // Batch gate table (one entry per GROUP op, in op order); gate_of_op maps an
+    // op index to its entry.
+    int upload_batch_gates(const std::vector<Op>& ops, const std::vector<GArgs>& groups,
+                           std::vector<int>& gate_of_op) {
         std::vector<BatchGate> bg;
-        std::vector<int> gate_of_op(ops.size(), -1);
+        gate_of_op.assign(ops.size(), -1);
         for (size_t o = 0; o < ops.size(); o++) {
             if (ops[o].type != Op::GROUP) continue;
             const GArgs& ga = groups[ops[o].idx];
@@ -984,7 +1037,124 @@ struct Engine {
             gate_of_op[o] = (int)bg.size();
             bg.push_back(b);
         }
-        rc = upload(ctx->d_bgates, ctx->bgates_cap, bg);
+        return upload(ctx->d_bgates, ctx->bgates_cap, bg);
+    }
+
+    // ---------------------------------------------------------------------
+    // batched instances: the op list as a list of steps (AdjRecord)
+    // ---------------------------------------------------------------------
+    // Splits the schedule into steps: Clifford ranges between commuting runs
+    // and orbit batches (every run goes through the orbit path).
+    static int build_records(const std::vector<Op>& ops, const std::vector<TruncArgs>& truncs,
+                             const std::vector<BatchInfo>& batches, const std::vector<int>& gate_of_op,
+                             std::vector<AdjRecord>& recs, std::string& err) {
+        recs.clear();
+        size_t pos = 0;
+        auto cliff = [&](size_t a, size_t b) -> bool {
+            for (size_t o = a; o < b; o++)
+                if (ops[o].type != Op::CLIFF) {
+                    err = "batched propagation: unexpected op outside a commuting run";
+                    return false;
+                }
+            if (a < b) {
+                AdjRecord r{};
+                r.type = AdjRecord::CLIFF;
+                r.op_begin = a;
+                r.op_end = b;
+                recs.push_back(r);
+            }
+            return true;
+        };
+        for (const BatchInfo& b : batches) {
+            if (b.trunc >= 0 && ops[b.trunc].topk > 0) {
+                err = "batched propagation does not support top-k truncation";
+                return -1;
+            }
+            const size_t end = b.trunc >= 0 ? (size_t)b.trunc + 1 : (size_t)(b.first + b.nrot);
+            if (!cliff(pos, (size_t)b.first)) return -1;
+            int done = 0;
+            while (done < b.nrot) {
+                const int k = std::min(kMaxBatchGates, b.nrot - done);
+                AdjRecord r{};
+                r.type = AdjRecord::ORBIT;
+                r.g0 = gate_of_op[b.first + done];
+                r.k = k;
+                if (done + k == b.nrot && b.trunc >= 0) {
+                    r.has_trunc = true;
+                    r.trunc = truncs[ops[b.trunc].idx];
+                }
+                recs.push_back(r);
+                done += k;
+            }
+            pos = end;
+        }
+        if (!cliff(pos, ops.size())) return -1;
+        return 0;
+    }
+
+    // Copies the current (dense) store into a checkpoint of the step.
+    int snapshot(AdjRecord& r) {
+        const u64 n = ctx->h_ctr->n;
+        if (n != ctx->h_ctr->alive) return set_err(ctx, FFG_ERR_STATE, "batched propagation: sparse store at a step");
+        r.n_in = n;
+        const size_t m = std::max<u64>(n, 1);
+        CK(cudaMalloc(&r.key, (size_t)KW * m * 8));
+        CK(cudaMalloc(&r.re, m * 8));
+        for (int w = 0; w < KW; w++)
+            CK(cudaMemcpyAsync(r.key + (size_t)w * n, cur.v.key + (size_t)w * cap, n * 8, cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+        CK(cudaMemcpyAsync(r.re, cur.v.re, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+        return FFG_OK;
+    }
+
+    // Loads a checkpoint (store planes, dense) as the live store.
+    int restore(const AdjRecord& r) {
+        const u64 n = r.n_in;
+        cap = pow2_at_least(std::max<u64>((u64)n * 4, 1u << 16));
+        int rc = ensure_buf(ctx, ctx->buf[0], store_bytes(KW, CPLX, cap));
+        if (rc) return rc;
+        active = 0;
+        cur = carve(ctx->buf[0], KW, CPLX, cap);
+        for (int w = 0; w < KW; w++)
+            CK(cudaMemcpyAsync(cur.v.key + (size_t)w * cap, r.key + (size_t)w * n, n * 8, cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+        CK(cudaMemcpyAsync(cur.v.re, r.re, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemsetAsync(cur.v.dead, 0, cap, ctx->stream));
+        DevCounters h = *ctx->h_ctr;
+        h.n = n;
+        h.alive = n;
+        h.overflow = 0;
+        h.error = 0;
+        *ctx->h_ctr = h;
+        CK(cudaMemcpyAsync(ctx->d_ctr, ctx->h_ctr, sizeof(DevCounters), cudaMemcpyHostToDevice, ctx->stream));
+        reindex(cur, 0);
+        index_valid = true;
+        return sync_counters();
+    }
+
+    // Runs one step forward on the live store.
+    int exec_record(const AdjRecord& r, int maxdeg) {
+        if (r.type == AdjRecord::CLIFF) {
+            int rc = exec_persistent(r.op_begin, r.op_end);
+            if (!rc) rc = sync_counters();
+            return rc;
+        }
+        int rc = sync_counters();
+        if (rc) return rc;
+        rc = exec_orbit_batch(r.g0, r.k, r.has_trunc ? &r.trunc : nullptr, maxdeg);
+        if (rc == 1) return set_err(ctx, FFG_ERR_STATE, "batched propagation: orbit group larger than 2^26 terms");
+        return rc;
+    }
+
+    // Pauli batched runs: long commuting runs go through the batch-orbit path,
+    // everything else through persistent per-gate runs.
+    int run_mixed(const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
+                  const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups,
+                  const std::vector<BatchInfo>& batches, int maxdeg) {
+        int rc = prepare_persistent(ops, rots, truncs, groups);
+        if (rc) return rc;
+        std::vector<int> gate_of_op;
+        rc = upload_batch_gates(ops, groups, gate_of_op);
         if (rc) return rc;
         size_t pos = 0;  // next op to execute
         for (const BatchInfo& b : batches) {
@@ -1186,12 +1356,16 @@ void build_pauli_ops(const ffg_pauli_gate* g, size_t ng, const ffg_pauli_params&
                     add_cliff(i + 1, cb + 1);
                     pending = false;
                 }
+                const int first = (int)ops.size();
                 if (groups)
                     add_groups(g, std::vector<size_t>{(size_t)i}, p, nw, dmax, ops, *groups);
                 else
                     add_rot((size_t)i);
+                const int nrot = (int)ops.size() - first;
                 if (batches) batches->push_back(1);
+                const size_t before = ops.size();
                 add_trunc(rot_count);
+                if (binfo) binfo->push_back({first, nrot, ops.size() > before ? (int)before : -1});
                 rot_count++;
             }
         }
@@ -1297,6 +1471,294 @@ int upload_cliffords(ffg_ctx* ctx, const ffg_pauli_gate* g, size_t ng) {
     if (ng) CK(cudaMemcpyAsync(ctx->d_cliff, h.data(), ng * sizeof(CliffordOp), cudaMemcpyHostToDevice,
                                ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return FFG_OK;
+}
+
+
+void free_record(AdjRecord& r) {
+    if (r.key) cudaFree(r.key);
+    if (r.re) cudaFree(r.re);
+    r.key = nullptr;
+    r.re = nullptr;
+}
+
+// Forward pass of a batched propagation on encoded keys (caller layout).
+template <int KW>
+int batch_forward(ffg_batch* h, const uint64_t* keys, const double* re, size_t n, double* expect) {
+    ffg_ctx* ctx = h->ctx;
+    Engine<KW, false, true> E(ctx);
+    int rc = E.load(keys, re, nullptr, n, 0, 0);
+    if (rc) return rc;
+    rc = E.prepare_persistent(h->ops, h->rots, h->truncs, h->groups);
+    if (rc) return rc;
+    std::vector<int> gate_of_op;
+    rc = E.upload_batch_gates(h->ops, h->groups, gate_of_op);
+    if (rc) return rc;
+    std::string err;
+    if (E.build_records(h->ops, h->truncs, h->binfo, gate_of_op, h->recs, err)) return set_err(ctx, FFG_ERR_ARG, err);
+    ctx->batch = &h->bc;
+    for (size_t r = 0; r < h->recs.size() && !rc; r++) {
+        if (h->every > 0 && r % (size_t)h->every == 0) rc = E.snapshot(h->recs[r]);
+        if (!rc) {
+            h->recs[r].n_in = ctx->h_ctr->n;
+            rc = E.exec_record(h->recs[r], h->maxdeg);
+        }
+    }
+    if (!rc) rc = E.finish();
+    ctx->batch = nullptr;
+    if (rc) return rc;
+    ctx->prof.apps = (int64_t)ctx->h_ctr->apps;
+    ctx->prof.emits = (int64_t)ctx->h_ctr->emits;
+    ctx->prof.peak_terms = (int64_t)ctx->h_ctr->peak;
+    ctx->prof.final_terms = (int64_t)ctx->h_ctr->n;
+    // keep the final term set
+    const u64 fn = ctx->h_ctr->n;
+    const size_t m = std::max<u64>(fn, 1);
+    h->fn = fn;
+    CK(cudaMalloc(&h->fkey, (size_t)KW * m * 8));
+    CK(cudaMalloc(&h->fre, m * 8));
+    for (int w = 0; w < KW; w++)
+        CK(cudaMemcpyAsync(h->fkey + (size_t)w * fn, E.cur.v.key + (size_t)w * E.cap, fn * 8,
+                           cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(h->fre, E.cur.v.re, fn * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    // per-instance <0|O|0>
+    double* d_exp = nullptr;
+    CK(cudaMalloc(&d_exp, h->ninst * 8));
+    CK(cudaMemsetAsync(d_exp, 0, h->ninst * 8, ctx->stream));
+    if (fn) {
+        StoreView v{};
+        v.key = h->fkey;
+        v.re = h->fre;
+        v.cap = fn;
+        batch_expect<KW / 2><<<grid_for(ctx, fn), kBlock, 0, ctx->stream>>>(
+            v, fn, h->xmask[0], h->xmask[1], h->bc.inst_plane, h->bc.inst_shift, h->bc.inst_mask, d_exp, nullptr,
+            nullptr);
+        ctx->prof.kernel_launches++;
+    }
+    cudaError_t e = cudaMemcpyAsync(expect, d_exp, h->ninst * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_exp);
+    if (e != cudaSuccess) return set_err(ctx, FFG_ERR_CUDA, cudaGetErrorString(e));
+    return FFG_OK;
+}
+
+// Device buffers of the backward pass.
+struct AdjBufs {
+    double* abar_out = nullptr;
+    u64* slots_out = nullptr;
+    size_t slots_out_n = 0;
+    double* abar_in = nullptr;
+    u64* slots_in = nullptr;
+    size_t slots_in_n = 0;
+    double* grad = nullptr;
+    double* w = nullptr;
+    int2* segs = nullptr;
+    u32* err = nullptr;
+    ~AdjBufs() {
+        for (void* p : {(void*)abar_out, (void*)slots_out, (void*)abar_in, (void*)slots_in, (void*)grad, (void*)w,
+                        (void*)segs, (void*)err})
+            if (p) cudaFree(p);
+    }
+};
+
+// Index over a dense term set (kw planes of n keys, stride n) in `slots`.
+template <int KW>
+int index_dense(ffg_ctx* ctx, StoreView& v, u64*& slots, size_t& slots_n, u32* err) {
+    const u64 n = v.cap;
+    const size_t need = 2 * pow2_at_least(std::max<u64>(n, 16));
+    if (slots_n < need) {
+        if (slots) CK(cudaFree(slots));
+        slots = nullptr;
+        CK(cudaMalloc(&slots, need * 8));
+        slots_n = need;
+    }
+    v.slots = slots;
+    v.hmask = need - 1;
+    clear_slots_kernel<<<grid_for(ctx, need), kBlock, 0, ctx->stream>>>(slots, need);
+    if (n) adj_index<KW><<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(v, n, err);
+    CK(cudaGetLastError());
+    return FFG_OK;
+}
+
+template <int KW>
+int batch_adjoint(ffg_batch* h, const double* weights, double* grad_theta, double* grad_coef) {
+    constexpr int NW = KW / 2;
+    ffg_ctx* ctx = h->ctx;
+    CK(cudaSetDevice(ctx->device));
+    if (h->every <= 0) return set_err(ctx, FFG_ERR_ARG, "the propagation kept no checkpoints (checkpoint_every = 0)");
+    Engine<KW, false, true> E(ctx);
+    int rc = upload_cliffords(ctx, h->gates.data(), h->gates.size());
+    if (rc) return rc;
+    rc = E.prepare_persistent(h->ops, h->rots, h->truncs, h->groups);
+    if (rc) return rc;
+    std::vector<int> gate_of_op;
+    rc = E.upload_batch_gates(h->ops, h->groups, gate_of_op);
+    if (rc) return rc;
+    const size_t ninst = h->ninst;
+    size_t nbg = 0;
+    for (const Op& o : h->ops) nbg += o.type == Op::GROUP;
+    AdjBufs B;
+    CK(cudaMalloc(&B.err, 8));
+    CK(cudaMemsetAsync(B.err, 0, 8, ctx->stream));
+    CK(cudaMalloc(&B.w, ninst * 8));
+    CK(cudaMemcpyAsync(B.w, weights, ninst * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMalloc(&B.grad, std::max<size_t>(nbg * ninst, 1) * 8));
+    CK(cudaMemsetAsync(B.grad, 0, std::max<size_t>(nbg * ninst, 1) * 8, ctx->stream));
+    // abar of the final term set
+    StoreView out{};
+    out.key = h->fkey;
+    out.re = h->fre;
+    out.cap = h->fn;
+    CK(cudaMalloc(&B.abar_out, std::max<u64>(h->fn, 1) * 8));
+    rc = index_dense<KW>(ctx, out, B.slots_out, B.slots_out_n, B.err);
+    if (rc) return rc;
+    if (h->fn)
+        batch_expect<NW><<<grid_for(ctx, h->fn), kBlock, 0, ctx->stream>>>(
+            out, h->fn, h->xmask[0], h->xmask[1], h->bc.inst_plane, h->bc.inst_shift, h->bc.inst_mask, nullptr, B.w,
+            B.abar_out);
+    const size_t warp_smem = (size_t)kAdjWarps * adj_table_bytes<KW>(kAdjWarpCap, kAdjWarpGates);
+    CK(cudaFuncSetAttribute(adj_orbit_warp<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warp_smem));
+    ctx->batch = &h->bc;
+    const int R = (int)h->recs.size();
+    for (int r = R - 1; r >= 0 && !rc; r--) {
+        AdjRecord& rec = h->recs[r];
+        if (!rec.key) {
+            // recompute the segment from the last checkpoint before r
+            int c = r;
+            while (c > 0 && !h->recs[c].key) c--;
+            if (!h->recs[c].key) return set_err(ctx, FFG_ERR_STATE, "adjoint: no checkpoint before step");
+            rc = E.restore(h->recs[c]);
+            for (int q = c; q < r && !rc; q++) {
+                if (q > c) {
+                    rc = E.snapshot(h->recs[q]);
+                    h->recs[q].temp = true;
+                }
+                if (!rc) rc = E.exec_record(h->recs[q], h->maxdeg);
+            }
+            if (!rc) rc = E.sync_counters();
+            if (!rc) {
+                rc = E.snapshot(rec);
+                rec.temp = true;
+            }
+            if (rc) break;
+        }
+        const u64 n_in = rec.n_in;
+        StoreView in{};
+        in.key = rec.key;
+        in.re = rec.re;
+        in.cap = n_in;
+        CK(cudaMalloc(&B.abar_in, std::max<u64>(n_in, 1) * 8));
+        if (n_in && rec.type == AdjRecord::CLIFF) {
+            std::vector<int2> segs;
+            for (size_t o = rec.op_begin; o < rec.op_end; o++) segs.push_back(make_int2(h->ops[o].begin, h->ops[o].end));
+            CK(cudaMalloc(&B.segs, segs.size() * sizeof(int2)));
+            CK(cudaMemcpyAsync(B.segs, segs.data(), segs.size() * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream));
+            adj_clifford<NW><<<grid_for(ctx, n_in), kBlock, 0, ctx->stream>>>(
+                in, n_in, ctx->d_cliff, B.segs, (int)segs.size(), out, B.abar_out, B.abar_in, B.err);
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(ctx->stream));
+            CK(cudaFree(B.segs));
+            B.segs = nullptr;
+        } else if (n_in) {
+            const u64 cap_in = std::max<u64>(n_in, 1024);
+            OrbitScratch sc = E.carve_scratch(cap_in);
+            if (!sc.amask) return set_err(ctx, FFG_ERR_CUDA, "adjoint: orbit scratch allocation failed");
+            // classification needs an output store for the untouched terms (discarded here)
+            const u64 dcap = pow2_at_least(std::max<u64>(n_in, 1024));
+            rc = ensure_buf(ctx, ctx->buf[0], store_bytes(KW, false, dcap));
+            if (rc) break;
+            Store dummy = carve(ctx->buf[0], KW, false, dcap);
+            AdjArgs A{};
+            OrbitBatchArgs& a = A.a;
+            a.gates = ctx->d_bgates + rec.g0;
+            a.k = rec.k;
+            a.maxdeg = h->maxdeg;
+            a.thr = rec.has_trunc ? rec.trunc.thr : 0;
+            a.tau = rec.has_trunc ? rec.trunc.tau : 0.0;
+            a.max_xweight = rec.has_trunc ? rec.trunc.max_xweight : -1;
+            a.route_big = ctx->orbit_route_big;
+            a.inst_cs = h->bc.d_inst_cs + (size_t)rec.g0 * ninst;
+            a.ninst = (u32)ninst;
+            a.inst_plane = h->bc.inst_plane;
+            a.inst_shift = h->bc.inst_shift;
+            a.inst_mask = h->bc.inst_mask;
+            A.out = out;
+            A.abar_out = B.abar_out;
+            A.abar_in = B.abar_in;
+            A.grad = B.grad + (size_t)rec.g0 * ninst;
+            A.err = B.err;
+            CK(cudaMemsetAsync(ctx->d_oc, 0, sizeof(OrbitCounters), ctx->stream));
+            CK(cudaMemsetAsync(sc.gslots, 0xff, (sc.gmask + 1) * 8, ctx->stream));
+            const int g = grid_for(ctx, n_in);
+            orbit_classify<NW, false><<<g, kBlock, 0, ctx->stream>>>(in, n_in, dummy.v, sc, ctx->d_oc, a);
+            orbit_group<KW><<<g, kBlock, 0, ctx->stream>>>(n_in, sc, ctx->d_oc);
+            orbit_offsets<<<1, 1024, 0, ctx->stream>>>(sc, ctx->d_oc);
+            orbit_scatter<<<g, kBlock, 0, ctx->stream>>>(n_in, sc);
+            adj_passthrough<KW><<<g, kBlock, 0, ctx->stream>>>(in, n_in, sc, A);
+            adj_orbit_warp<NW><<<ctx->num_sms * 2, 32 * kAdjWarps, warp_smem, ctx->stream>>>(in, sc, ctx->d_oc, A);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(ctx->h_oc, ctx->d_oc, sizeof(OrbitCounters), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            if (ctx->h_oc->error) return set_err(ctx, FFG_ERR_STATE, "adjoint: orbit grouping index overrun");
+            u32 nbig = ctx->h_oc->nbig;
+            u32* list = sc.big;
+            u32* other = E.retry_list;
+            u32 tcap = 4096;
+            while (nbig > 0) {
+                if (tcap > (1u << 22)) return set_err(ctx, FFG_ERR_STATE, "adjoint: orbit group larger than 2^22 terms");
+                const u32 grid = std::min<u32>(nbig, (u32)ctx->num_sms);
+                const u64 region = adj_table_bytes<KW>(tcap, (u32)rec.k);
+                rc = ensure_buf(ctx, ctx->bigpool, region * grid);
+                if (rc) return rc;
+                CK(cudaMemsetAsync(E.nretry, 0, 4, ctx->stream));
+                adj_orbit_block<NW><<<grid, 1024, 0, ctx->stream>>>(in, sc, A, ctx->bigpool.p, region, tcap,
+                                                                    (u32)rec.k, list, nbig, other, E.nretry);
+                CK(cudaGetLastError());
+                u32 hr = 0;
+                CK(cudaMemcpyAsync(&hr, E.nretry, 4, cudaMemcpyDeviceToHost, ctx->stream));
+                CK(cudaStreamSynchronize(ctx->stream));
+                std::swap(list, other);
+                nbig = hr;
+                tcap *= 4;
+            }
+        }
+        // this step's input becomes the next step's output side
+        rc = index_dense<KW>(ctx, in, B.slots_in, B.slots_in_n, B.err);
+        if (rc) break;
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaFree(B.abar_out));
+        B.abar_out = B.abar_in;
+        B.abar_in = nullptr;
+        std::swap(B.slots_out, B.slots_in);
+        std::swap(B.slots_out_n, B.slots_in_n);
+        out = in;
+        // recomputed checkpoints after this step are no longer needed (this
+        // step's own checkpoint is the output side of the next one)
+        for (int q = r + 1; q < R; q++)
+            if (h->recs[q].temp) {
+                free_record(h->recs[q]);
+                h->recs[q].temp = false;
+            }
+    }
+    ctx->batch = nullptr;
+    for (AdjRecord& q : h->recs)
+        if (q.temp) {
+            free_record(q);
+            q.temp = false;
+        }
+    if (rc) return rc;
+    u32 herr[2] = {0, 0};
+    CK(cudaMemcpy(herr, B.err, 8, cudaMemcpyDeviceToHost));
+    if (herr[0] & 2u) return set_err(ctx, FFG_ERR_STATE, "adjoint: index probe overrun");
+    if (grad_coef && h->n_input) {
+        if (out.cap != h->n_input) return set_err(ctx, FFG_ERR_STATE, "adjoint: input term count mismatch");
+        CK(cudaMemcpy(grad_coef, B.abar_out, h->n_input * 8, cudaMemcpyDeviceToHost));
+    }
+    std::vector<double> g(nbg * ninst);
+    if (!g.empty()) CK(cudaMemcpy(g.data(), B.grad, g.size() * 8, cudaMemcpyDeviceToHost));
+    // batch gate b is the b-th rotation in application order = rotation nrot-1-b in circuit order
+    for (size_t i = 0; i < ninst; i++)
+        for (size_t b = 0; b < nbg; b++) grad_theta[i * h->nrot + (h->nrot - 1 - b)] = g[b * ninst + i];
     return FFG_OK;
 }
 
@@ -1787,3 +2249,190 @@ int64_t ffg_pauli_schedule(const ffg_pauli_gate* gates, size_t ngates, int batch
     return (int64_t)b.size();
 }
 
+
+// ---------------------------------------------------------------------------
+// batched instances and the adjoint
+// ---------------------------------------------------------------------------
+int ffg_pauli_propagate_batched(ffg_ctx* ctx, const uint64_t* keys, const double* re, size_t n,
+                                const ffg_pauli_gate* gates, size_t ngates, const ffg_pauli_params* params,
+                                const ffg_batch_params* bp, double* expect, ffg_batch** out) {
+    if (!ctx || !params || !bp || !expect || (n && (!keys || !re)) || (ngates && !gates)) return FFG_ERR_ARG;
+    if (out) *out = nullptr;
+    const size_t ninst = bp->ninst;
+    if (ninst == 0 || !bp->offsets) return set_err(ctx, FFG_ERR_ARG, "batched propagation: no instances");
+    if (bp->offsets[0] != 0 || (size_t)bp->offsets[ninst] != n)
+        return set_err(ctx, FFG_ERR_ARG, "batched propagation: offsets must start at 0 and end at n");
+    for (size_t i = 0; i < ninst; i++)
+        if (bp->offsets[i + 1] < bp->offsets[i])
+            return set_err(ctx, FFG_ERR_ARG, "batched propagation: offsets must be non-decreasing");
+    if (params->topk > 0) return set_err(ctx, FFG_ERR_ARG, "batched propagation does not support top-k truncation");
+    if (params->max_xweight >= 0)
+        return set_err(ctx, FFG_ERR_ARG, "batched propagation does not support X-weight truncation");
+    if (bp->checkpoint_every < 0) return set_err(ctx, FFG_ERR_ARG, "checkpoint_every must be >= 0");
+    if (ctx->group_d != 1 || !ctx->orbit || !ctx->persistent)
+        return set_err(ctx, FFG_ERR_ARG, "batched propagation needs the orbit and persistent paths (FFG_* overrides)");
+    try {
+        auto t0 = std::chrono::steady_clock::now();
+        reset_profile(ctx);
+        CK(cudaSetDevice(ctx->device));
+        // qubits in use
+        int nq = 0;
+        size_t nrot = 0;
+        auto use_bits = [&](uint64_t w, int word) {
+            if (w) nq = std::max(nq, 64 * word + 64 - __builtin_clzll(w));
+        };
+        for (size_t i = 0; i < ngates; i++) {
+            const ffg_pauli_gate& G = gates[i];
+            if (G.kind < FFG_ROT || G.kind > FFG_CZ)
+                return set_err(ctx, FFG_ERR_ARG, "gate " + std::to_string(i) + ": unknown kind");
+            if (G.kind == FFG_ROT) {
+                nrot++;
+                for (int w = 0; w < 2; w++) {
+                    use_bits(G.x[w], w);
+                    use_bits(G.z[w], w);
+                }
+            } else {
+                const bool two = G.kind >= FFG_CNOT;
+                if (G.q0 < 0 || G.q0 >= 128 || (two && (G.q1 < 0 || G.q1 >= 128)))
+                    return set_err(ctx, FFG_ERR_ARG, "gate " + std::to_string(i) + ": qubit index out of range");
+                nq = std::max(nq, G.q0 + 1);
+                if (two) nq = std::max(nq, G.q1 + 1);
+            }
+        }
+        for (size_t i = 0; i < n; i++)
+            for (int w = 0; w < 2; w++) {
+                use_bits(keys[w * n + i], w);
+                use_bits(keys[(2 + w) * n + i], w);
+            }
+        int b = 1;
+        while (((size_t)1 << b) < ninst) b++;
+        // instance code: x bits [shift, shift+b) of caller word `word`, complement in z
+        int word, shift;
+        if (nq + b <= 64) {
+            word = 0;
+            shift = nq;
+        } else if (nq <= 64) {
+            word = 1;
+            shift = 0;
+        } else if (nq + b <= 128) {
+            word = 1;
+            shift = nq - 64;
+        } else {
+            return set_err(ctx, FFG_ERR_ARG, "batched propagation: no free key bits for the instance code");
+        }
+        const bool wide = word == 1 || nq > 64;
+        const int kw = wide ? 4 : 2;
+        const u64 imask = (b == 64) ? ~0ull : ((1ull << b) - 1);
+        auto* h = new ffg_batch();
+        h->ctx = ctx;
+        h->kw = kw;
+        h->ninst = ninst;
+        h->nrot = nrot;
+        h->n_input = n;
+        h->every = bp->checkpoint_every;
+        h->gates.assign(gates, gates + ngates);
+        h->inst_word = word;
+        for (int w = 0; w < 2; w++) {
+            const int lo = 64 * w, hi = 64 * w + 64;
+            const int q1 = std::min(nq, hi);
+            u64 m = 0;
+            for (int q = lo; q < q1; q++) m |= 1ull << (q - lo);
+            h->xmask[w] = m;
+        }
+        h->maxdeg = params->maxdegree + b;
+        h->bc.ninst = (u32)ninst;
+        h->bc.inst_plane = wide ? word : 0;  // x plane of that word in store order
+        h->bc.inst_shift = shift;
+        h->bc.inst_mask = imask;
+        std::unique_ptr<ffg_batch, void (*)(ffg_batch*)> guard(h, ffg_batch_free);
+        // encoded keys
+        std::vector<uint64_t> ek(keys, keys + 4 * n);
+        for (size_t i = 0; i < ninst; i++)
+            for (int64_t t = bp->offsets[i]; t < bp->offsets[i + 1]; t++) {
+                ek[(size_t)word * n + t] |= (u64)i << shift;
+                ek[(size_t)(2 + word) * n + t] |= ((~(u64)i) & imask) << shift;
+            }
+        // schedule with the instance bits counted in the degree filter
+        ffg_pauli_params p = *params;
+        p.maxdegree = h->maxdeg;
+        build_pauli_ops(gates, ngates, p, wide ? 2 : 1, h->ops, h->rots, h->truncs, nullptr, &h->groups, 1,
+                        &h->binfo);
+        size_t nbg = 0;
+        for (const Op& o : h->ops) nbg += o.type == Op::GROUP;
+        if (nbg != nrot) return set_err(ctx, FFG_ERR_STATE, "batched propagation: schedule does not cover every rotation");
+        ctx->prof.n_gates = (int64_t)nrot;
+        // per-instance (cos, sin); batch gate b is circuit rotation nrot-1-b
+        std::vector<double> theta_of_rot;
+        for (size_t i = 0; i < ngates; i++)
+            if (gates[i].kind == FFG_ROT) theta_of_rot.push_back(gates[i].theta);
+        std::vector<double2> cs(nbg * ninst);
+        for (size_t bgi = 0; bgi < nbg; bgi++) {
+            const size_t rot = nrot - 1 - bgi;
+            for (size_t i = 0; i < ninst; i++) {
+                const double th = bp->thetas ? bp->thetas[i * nrot + rot] : theta_of_rot[rot];
+                cs[bgi * ninst + i] = make_double2(std::cos(th), std::sin(th));
+            }
+        }
+        CK(cudaMalloc(&h->d_inst_cs, std::max<size_t>(cs.size(), 1) * sizeof(double2)));
+        if (!cs.empty())
+            CK(cudaMemcpy(h->d_inst_cs, cs.data(), cs.size() * sizeof(double2), cudaMemcpyHostToDevice));
+        h->bc.d_inst_cs = h->d_inst_cs;
+        int rc = upload_cliffords(ctx, gates, ngates);
+        if (rc) return rc;
+        rc = kw == 2 ? batch_forward<2>(h, ek.data(), re, n, expect) : batch_forward<4>(h, ek.data(), re, n, expect);
+        ctx->prof.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (rc) return rc;
+        if (out) *out = guard.release();
+        return FFG_OK;
+    } catch (const std::exception& ex) {
+        return set_err(ctx, FFG_ERR_STATE, ex.what());
+    }
+}
+
+size_t ffg_batch_size(const ffg_batch* h) { return h ? (size_t)h->fn : 0; }
+
+int ffg_batch_copy(const ffg_batch* h, uint64_t* keys, double* re, int64_t* inst) {
+    if (!h || (h->fn && (!keys || !re))) return FFG_ERR_ARG;
+    ffg_ctx* ctx = h->ctx;
+    const size_t n = h->fn;
+    if (!n) return FFG_OK;
+    std::vector<u64> k((size_t)h->kw * n);
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpy(k.data(), h->fkey, k.size() * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(re, h->fre, n * 8, cudaMemcpyDeviceToHost));
+    const int nw = h->kw / 2;
+    const u64 code = h->bc.inst_mask << h->bc.inst_shift;
+    for (size_t i = 0; i < n; i++) {
+        u64 x[2] = {k[i], nw > 1 ? k[n + i] : 0};
+        u64 z[2] = {k[(size_t)nw * n + i], nw > 1 ? k[(size_t)(nw + 1) * n + i] : 0};
+        const int wd = h->inst_word;
+        if (inst) inst[i] = (int64_t)((x[wd] >> h->bc.inst_shift) & h->bc.inst_mask);
+        x[wd] &= ~code;
+        z[wd] &= ~code;
+        keys[i] = x[0];
+        keys[n + i] = x[1];
+        keys[2 * n + i] = z[0];
+        keys[3 * n + i] = z[1];
+    }
+    return FFG_OK;
+}
+
+int ffg_batch_adjoint(ffg_batch* h, const double* weights, double* grad_theta, double* grad_coef) {
+    if (!h || !weights || !grad_theta) return FFG_ERR_ARG;
+    try {
+        return h->kw == 2 ? batch_adjoint<2>(h, weights, grad_theta, grad_coef)
+                          : batch_adjoint<4>(h, weights, grad_theta, grad_coef);
+    } catch (const std::exception& ex) {
+        return set_err(h->ctx, FFG_ERR_STATE, ex.what());
+    }
+}
+
+void ffg_batch_free(ffg_batch* h) {
+    if (!h) return;
+    if (h->ctx) cudaSetDevice(h->ctx->device);
+    for (AdjRecord& r : h->recs) free_record(r);
+    if (h->fkey) cudaFree(h->fkey);
+    if (h->fre) cudaFree(h->fre);
+    if (h->d_inst_cs) cudaFree(h->d_inst_cs);
+    delete h;
+}

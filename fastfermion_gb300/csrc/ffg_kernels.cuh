@@ -311,6 +311,65 @@ __device__ __forceinline__ void set_bit(u64 (&w)[NW], int i, u64 b) {
     w[i >> 6] = (w[i >> 6] & ~(1ull << (i & 63))) | (b << (i & 63));
 }
 
+// Maps the key (x, z) through the Clifford gates ops[nops-1] .. ops[0] (the
+// Heisenberg order) and returns the number of sign flips.
+template <int NW>
+__device__ __forceinline__ int clifford_map(u64 (&x)[NW], u64 (&z)[NW], const CliffordOp* ops, int nops) {
+    int flips = 0;
+    for (int g = nops - 1; g >= 0; g--) {
+        const CliffordOp o = ops[g];
+        const int a = o.q0, b = o.q1;
+        switch (o.kind) {
+            case kH: {
+                const u64 xa = bit_at<NW>(x, a), za = bit_at<NW>(z, a);
+                set_bit<NW>(x, a, za);
+                set_bit<NW>(z, a, xa);
+                flips += (int)(xa & za);
+                break;
+            }
+            case kS: {
+                const u64 xa = bit_at<NW>(x, a), za = bit_at<NW>(z, a);
+                set_bit<NW>(z, a, xa ^ za);
+                flips += (int)(xa & (za ^ 1ull));
+                break;
+            }
+            case kCNOT: {
+                const u64 xa = bit_at<NW>(x, a), xb = bit_at<NW>(x, b);
+                const u64 za = bit_at<NW>(z, a), zb = bit_at<NW>(z, b);
+                set_bit<NW>(x, b, xa ^ xb);
+                set_bit<NW>(z, a, za ^ zb);
+                flips += (int)(xa & zb & ((za ^ xb) ^ 1ull));
+                break;
+            }
+            case kSWAP: {
+                const u64 xa = bit_at<NW>(x, a), xb = bit_at<NW>(x, b);
+                const u64 za = bit_at<NW>(z, a), zb = bit_at<NW>(z, b);
+                set_bit<NW>(x, a, xb);
+                set_bit<NW>(x, b, xa);
+                set_bit<NW>(z, a, zb);
+                set_bit<NW>(z, b, za);
+                break;
+            }
+            case kCZ: {
+                const u64 xa = bit_at<NW>(x, a), xb = bit_at<NW>(x, b);
+                const u64 za = bit_at<NW>(z, a), zb = bit_at<NW>(z, b);
+                flips += (int)(xa & xb & (za ^ zb));
+                u64 m[NW];
+#pragma unroll
+                for (int w = 0; w < NW; w++) m[w] = 0;
+                m[a >> 6] |= xb << (a & 63);
+                m[b >> 6] |= xa << (b & 63);
+#pragma unroll
+                for (int w = 0; w < NW; w++) z[w] ^= m[w];
+                break;
+            }
+            default:
+                break;
+        }
+    }
+    return flips;
+}
+
 template <int NW, bool CPLX>
 __global__ void __launch_bounds__(kBlock) clifford_kernel(StoreView s, DevCounters* C,
                                                           const CliffordOp* ops, int nops, u32 op) {
@@ -326,58 +385,7 @@ __global__ void __launch_bounds__(kBlock) clifford_kernel(StoreView s, DevCounte
                 x[w] = s.key[(u64)w * s.cap + i];
                 z[w] = s.key[(u64)(NW + w) * s.cap + i];
             }
-            int flips = 0;
-            for (int g = nops - 1; g >= 0; g--) {
-                const CliffordOp o = ops[g];
-                const int a = o.q0, b = o.q1;
-                switch (o.kind) {
-                    case kH: {
-                        const u64 xa = bit_at<NW>(x, a), za = bit_at<NW>(z, a);
-                        set_bit<NW>(x, a, za);
-                        set_bit<NW>(z, a, xa);
-                        flips += (int)(xa & za);
-                        break;
-                    }
-                    case kS: {
-                        const u64 xa = bit_at<NW>(x, a), za = bit_at<NW>(z, a);
-                        set_bit<NW>(z, a, xa ^ za);
-                        flips += (int)(xa & (za ^ 1ull));
-                        break;
-                    }
-                    case kCNOT: {
-                        const u64 xa = bit_at<NW>(x, a), xb = bit_at<NW>(x, b);
-                        const u64 za = bit_at<NW>(z, a), zb = bit_at<NW>(z, b);
-                        set_bit<NW>(x, b, xa ^ xb);
-                        set_bit<NW>(z, a, za ^ zb);
-                        flips += (int)(xa & zb & ((za ^ xb) ^ 1ull));
-                        break;
-                    }
-                    case kSWAP: {
-                        const u64 xa = bit_at<NW>(x, a), xb = bit_at<NW>(x, b);
-                        const u64 za = bit_at<NW>(z, a), zb = bit_at<NW>(z, b);
-                        set_bit<NW>(x, a, xb);
-                        set_bit<NW>(x, b, xa);
-                        set_bit<NW>(z, a, zb);
-                        set_bit<NW>(z, b, za);
-                        break;
-                    }
-                    case kCZ: {
-                        const u64 xa = bit_at<NW>(x, a), xb = bit_at<NW>(x, b);
-                        const u64 za = bit_at<NW>(z, a), zb = bit_at<NW>(z, b);
-                        flips += (int)(xa & xb & (za ^ zb));
-                        u64 m[NW];
-#pragma unroll
-                        for (int w = 0; w < NW; w++) m[w] = 0;
-                        m[a >> 6] |= xb << (a & 63);
-                        m[b >> 6] |= xa << (b & 63);
-#pragma unroll
-                        for (int w = 0; w < NW; w++) z[w] ^= m[w];
-                        break;
-                    }
-                    default:
-                        break;
-                }
-            }
+            const int flips = clifford_map<NW>(x, z, ops, nops);
 #pragma unroll
             for (int w = 0; w < NW; w++) {
                 s.key[(u64)w * s.cap + i] = x[w];

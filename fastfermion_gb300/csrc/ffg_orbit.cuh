@@ -98,7 +98,34 @@ struct OrbitBatchArgs {
     double tau;
     int max_xweight;
     int route_big;  // groups with at least this many gates in A go straight to the block-level pass
+    // batched instances (null inst_cs: one instance, angles from `gates`).  The
+    // instance of a term is (key plane inst_plane >> inst_shift) & inst_mask;
+    // gate t of instance i uses inst_cs[t * ninst + i] = (cos, sin).
+    const double2* inst_cs;
+    u32 ninst;
+    int inst_plane;
+    int inst_shift;
+    u64 inst_mask;
 };
+
+// instance of the group represented by input position rep
+__device__ __forceinline__ u32 group_instance(const StoreView& in, const OrbitBatchArgs& a, u32 rep) {
+    if (!a.inst_cs) return 0;
+    return (u32)((in.key[(u64)a.inst_plane * in.cap + rep] >> a.inst_shift) & a.inst_mask);
+}
+
+// (cos, sin) of batch gate t for instance inst
+__device__ __forceinline__ void gate_cs(const OrbitBatchArgs& a, const BatchGate& G, int t, u32 inst,
+                                        double& c, double& s) {
+    if (a.inst_cs) {
+        const double2 v = a.inst_cs[(u64)t * a.ninst + inst];
+        c = v.x;
+        s = v.y;
+    } else {
+        c = G.c;
+        s = G.s;
+    }
+}
 
 template <int NW, bool CPLX>
 __device__ __forceinline__ bool survives(const u64* key, cplx c, const OrbitBatchArgs& a) {
@@ -377,6 +404,7 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
             T.flag = 0;
         }
         __syncwarp();
+        const u32 inst = group_instance(in, a, rep);
         // gates of A in batch order
         u64 A[kAW];
 #pragma unroll
@@ -387,10 +415,12 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                 const int t = 64 * wd + __ffsll((long long)bits) - 1;
                 bits &= bits - 1;
                 const BatchGate G = a.gates[t];
+                double gc, gs;
+                gate_cs(a, G, t, inst, gc, gs);
                 u64 P[KW];
 #pragma unroll
                 for (int w = 0; w < KW; w++) P[w] = G.p[w];
-                const cplx isin = {0.0, G.s};
+                const cplx isin = {0.0, gs};
                 const int cnt0 = (int)*(volatile unsigned int*)&T.cnt;
                 __syncwarp();
                 for (int m = lane; m < cnt0; m += 32) {
@@ -417,7 +447,7 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                     if (j >= 0 && j < cnt0) {
                         if (j < m) continue;  // the pair belongs to member j
                         const cplx cj = {T.re[j], CPLX ? T.im[j] : 0.0};
-                        cplx ni = cscale(ci, G.c), nj = cscale(cj, G.c);
+                        cplx ni = cscale(ci, gc), nj = cscale(cj, gc);
                         if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
                         if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
                         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
@@ -428,7 +458,7 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                             T.im[j] = nj.im;
                         }
                     } else {
-                        const cplx ni = cscale(ci, G.c);
+                        const cplx ni = cscale(ci, gc);
                         T.re[m] = ni.re;
                         if (CPLX) T.im[m] = ni.im;
                         if (dK <= a.maxdeg) {
@@ -639,16 +669,19 @@ __global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreVie
         __syncthreads();
         long long g_emits = 0, g_created = 0, g_xapps = 0;
         bool stop = false;
+        const u32 inst = group_instance(in, a, rep);
         for (int wd = 0; wd < kAW && !stop; wd++) {
             u64 bits = sc.amask[(u64)wd * sc.cap_in + rep];
             while (bits && !stop) {
                 const int t = 64 * wd + __ffsll((long long)bits) - 1;
                 bits &= bits - 1;
                 const BatchGate Gt = a.gates[t];
+                double gc, gs;
+                gate_cs(a, Gt, t, inst, gc, gs);
                 u64 P[KW];
 #pragma unroll
                 for (int w = 0; w < KW; w++) P[w] = Gt.p[w];
-                const cplx isin = {0.0, Gt.s};
+                const cplx isin = {0.0, gs};
                 const u32 cnt0 = *(volatile u32*)G.cnt;
                 __syncthreads();
                 for (u32 m = threadIdx.x; m < cnt0; m += blockDim.x) {
@@ -678,7 +711,7 @@ __global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreVie
                     if (j >= 0 && (u32)j < cnt0) {
                         if ((u32)j < m) continue;
                         const cplx cj = {tld<SM>(&G.re[j]), CPLX ? tld<SM>(&G.im[j]) : 0.0};
-                        cplx ni = cscale(ci, Gt.c), nj = cscale(cj, Gt.c);
+                        cplx ni = cscale(ci, gc), nj = cscale(cj, gc);
                         if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
                         if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
                         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
@@ -689,7 +722,7 @@ __global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreVie
                             G.im[j] = nj.im;
                         }
                     } else {
-                        const cplx ni = cscale(ci, Gt.c);
+                        const cplx ni = cscale(ci, gc);
                         G.re[m] = ni.re;
                         if (CPLX) G.im[m] = ni.im;
                         if (dK <= a.maxdeg) {

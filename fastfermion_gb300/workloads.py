@@ -89,3 +89,50 @@ def hubbard_step(lx=6, ly=6, t=1.0, u=4.0, dt=0.1):
 
 def hubbard_circuit(lx=6, ly=6, t=1.0, u=4.0, dt=0.1, steps=10):
     return hubbard_step(lx, ly, t, u, dt) * steps
+
+
+def hea_circuit(n=50, layers=8, theta=0.0):
+    """Hardware-efficient ansatz on an open chain: per layer RY(theta) on every
+    qubit, then CZ on the bonds (i, i+1).  Per-instance angles replace theta
+    (row i of ``hea_instances``' thetas, ROT gates in circuit order)."""
+    out = []
+    for _ in range(layers):
+        out += [("ROT", "Y", [q], theta) for q in range(n)]
+        out += [("CZ", q, q + 1) for q in range(n - 1)]
+    return out
+
+
+def hea_instances(ninst=256, n=50, layers=8, seed=0, max_terms=64, max_weight=4):
+    """Seeded instances of the batched ansatz workload: angles (ninst, layers*n)
+    from uniform[-pi, pi], and one observable per instance with a term count
+    drawn from 1..max_terms, each term a distinct random Pauli string of weight
+    1..max_weight on random qubits with an N(0, 1) coefficient.
+
+    Returns (thetas, [(keys (4, m) uint64, re (m,)) per instance])."""
+    rng = np.random.default_rng(seed)
+    thetas = rng.uniform(-math.pi, math.pi, size=(ninst, layers * n))
+    obs = []
+    for _ in range(ninst):
+        m = int(rng.integers(1, max_terms + 1))
+        seen = set()
+        keys = np.zeros((4, m), dtype=np.uint64)
+        re = rng.normal(size=m)
+        t = 0
+        while t < m:
+            w = int(rng.integers(1, max_weight + 1))
+            qs = rng.choice(n, size=w, replace=False)
+            x = z = 0
+            for q in qs:
+                p = int(rng.integers(1, 4))  # 1 X, 2 Y, 3 Z
+                if p in (1, 2):
+                    x |= 1 << int(q)
+                if p in (2, 3):
+                    z |= 1 << int(q)
+            if (x, z) in seen:
+                continue
+            seen.add((x, z))
+            keys[0, t], keys[1, t] = x & (2**64 - 1), x >> 64
+            keys[2, t], keys[3, t] = z & (2**64 - 1), z >> 64
+            t += 1
+        obs.append((keys, re))
+    return thetas, obs

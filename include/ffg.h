@@ -162,6 +162,51 @@ int ffg_result_fock_state(const ffg_result* r, const uint64_t* b /* [2] */, doub
 void ffg_result_free(ffg_result* r);
 
 /* -------------------------------------------------------------------------- */
+/* Batched instances and gradients.  No counterpart in the reference: its
+ * propagate runs one observable through one circuit and has no derivatives.
+ *
+ * ffg_pauli_propagate_batched propagates ninst observables through circuits
+ * that share the gate axes and Clifford gates of `gates` but have their own
+ * rotation angles, in one term store and one set of launches.  The terms of
+ * instance i are keys/re[offsets[i] .. offsets[i+1]) (caller layout [4][n],
+ * real coefficients; keys distinct within an instance).  Row i of thetas
+ * ([ninst][nrot], nrot = number of FFG_ROT gates, circuit order) holds
+ * instance i's angles; thetas == NULL uses gates[].theta for every instance.
+ * Truncation follows params exactly as ffg_pauli_propagate would for each
+ * instance alone (every instance's term set is bit-identical to that), except
+ * that top-k and X-weight truncation are not supported (FFG_ERR_ARG).
+ * expect[i] receives <0|O_i|0> (summation order not fixed).
+ * checkpoint_every = k >= 1 keeps the term set entering every k-th step
+ * (Clifford segment or commuting run) on the device so that
+ * ffg_batch_adjoint can run; the steps in between are recomputed during the
+ * backward pass.  out may be NULL when no handle is wanted. */
+typedef struct ffg_batch ffg_batch;
+
+typedef struct {
+    size_t ninst;
+    const int64_t* offsets;    /* [ninst + 1], offsets[0] = 0, offsets[ninst] = n */
+    const double* thetas;      /* [ninst][nrot] or NULL */
+    int32_t checkpoint_every;  /* 0: no adjoint */
+    int32_t pad;
+} ffg_batch_params;
+
+int ffg_pauli_propagate_batched(ffg_ctx* ctx, const uint64_t* keys, const double* re, size_t n,
+                                const ffg_pauli_gate* gates, size_t ngates, const ffg_pauli_params* params,
+                                const ffg_batch_params* bparams, double* expect, ffg_batch** out);
+/* Terms left over all instances. */
+size_t ffg_batch_size(const ffg_batch* b);
+/* Final terms: keys [4][n] (caller layout, instance code removed), re[n],
+ * inst[n] = instance of each term (may be NULL). */
+int ffg_batch_copy(const ffg_batch* b, uint64_t* keys, double* re, int64_t* inst);
+/* Reverse-mode derivative of F = sum_i weights[i] <0|O_i|0> with the
+ * truncation pattern of the forward pass held fixed:
+ * grad_theta[i * nrot + r] = dF / dthetas[i][r]; grad_coef[t] (may be NULL) =
+ * dF / d re[t] for the input terms.  Uses the context the handle was made
+ * with; may run any number of times. */
+int ffg_batch_adjoint(ffg_batch* b, const double* weights, double* grad_theta, double* grad_coef);
+void ffg_batch_free(ffg_batch* b);
+
+/* -------------------------------------------------------------------------- */
 /* Allocation-free rotations.  No counterpart in the reference: this entry
  * point exists for callers that cannot allocate device memory when they call
  * it (code running under stream capture, where cudaMalloc/cudaFree are not

@@ -358,6 +358,71 @@ def cases(ff):
     yield "hubbard_6x6_10steps", lambda: hub("hubbard_6x6_10steps", 6, 6, 10, 6, 1e-7)
 
 
+def obs_from_arrays(ff, keys, re):
+    """Reference PauliPolynomial of the terms keys (4, m) / re (m,)."""
+    p = ff.PauliPolynomial()
+    for t in range(re.size):
+        x = int(keys[0, t]) | (int(keys[1, t]) << 64)
+        z = int(keys[2, t]) | (int(keys[3, t]) << 64)
+        ops = []
+        for q in range(128):
+            a, b = (x >> q) & 1, (z >> q) & 1
+            if a or b:
+                ops.append((q, "X" if a and not b else ("Y" if a else "Z")))
+        p += ff.PauliPolynomial(ff.PauliString(ops)) * float(re[t])
+    return p
+
+
+def hea_instance_circuit(ff, n, layers, th):
+    spec = W.hea_circuit(n, layers)
+    out, r = [], 0
+    for s in spec:
+        if s[0] == "ROT":
+            out.append(ff.ROT(s[1], list(s[2]), float(th[r])))
+            r += 1
+        else:
+            out.append(mk(ff, s))
+    return out
+
+
+def hea_cases(ff):
+    """Batched-ansatz workload (256 instances x 50 qubits, 8 layers, W=6,
+    tau=1e-7): instances 0 and 1 run alone through the reference, and
+    parameter-shift derivatives of a small ansatz from the reference."""
+    thetas, obs = W.hea_instances(256)
+    for i in (0, 1):
+        nm = f"hea_50q_inst{i}"
+        yield nm, (lambda nm=nm, i=i: pauli_case(ff, nm, hea_instance_circuit(ff, 50, 8, thetas[i]),
+                                                  obs_from_arrays(ff, *obs[i]), maxdegree=6, mincoeff=1e-7))
+
+    def shift(nm, n, layers, ninst, seed, maxdegree, batched):
+        th, ob = W.hea_instances(ninst, n=n, layers=layers, seed=seed, max_terms=6, max_weight=3)
+        t0 = time.time()
+        f = np.zeros(ninst)
+        g = np.zeros_like(th)
+        for i in range(ninst):
+            o = obs_from_arrays(ff, *ob[i])
+
+            def ev(t):
+                return ff.propagate(hea_instance_circuit(ff, n, layers, t), o, maxdegree=maxdegree,
+                                    batched=batched).overlapwithzero().real
+            f[i] = ev(th[i])
+            for r in range(th.shape[1]):
+                tp, tm = th[i].copy(), th[i].copy()
+                tp[r] += math.pi / 2
+                tm[r] -= math.pi / 2
+                g[i, r] = 0.5 * (ev(tp) - ev(tm))
+        keys = np.concatenate([o[0] for o in ob], axis=1)
+        re = np.concatenate([o[1] for o in ob])
+        off = np.cumsum([0] + [o[1].size for o in ob]).astype(np.int64)
+        save(nm, kind="hea_shift", n=n, layers=layers, seed=seed, maxdegree=maxdegree, batched=batched,
+             thetas=th, obs_keys=keys, obs_re=re, offsets=off, expect=f, shift_grad=g)
+        print(f"{nm:32s} ninst={ninst} angles={th.shape[1]} {time.time() - t0:7.2f}s", flush=True)
+    yield "hea_shift_10q", lambda: shift("hea_shift_10q", 10, 3, 3, 7, 4, True)
+    yield "hea_shift_10q_unbatched", lambda: shift("hea_shift_10q_unbatched", 10, 3, 2, 8, 5, False)
+    yield "hea_shift_70q", lambda: shift("hea_shift_70q", 70, 2, 2, 9, 3, True)
+
+
 REF = "/root/reference"
 
 if __name__ == "__main__":
@@ -367,7 +432,7 @@ if __name__ == "__main__":
     a = ap.parse_args()
     REF = a.ref
     ff = load_reference(REF)
-    for name, fn in cases(ff):
+    for name, fn in list(cases(ff)) + list(hea_cases(ff)):
         if a.only and a.only not in name:
             continue
         fn()

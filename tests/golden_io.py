@@ -8,10 +8,14 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def fixture_names(kind=None, full_only=False):
+    """Propagation fixtures (kind "pauli" or "majorana"; other kinds, such as the
+    parameter-shift fixtures, are loaded by name)."""
     out = []
     for p in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         with np.load(p) as z:
             if kind and str(z["kind"]) != kind:
+                continue
+            if not kind and str(z["kind"]) not in ("pauli", "majorana"):
                 continue
             if full_only and "res_keys" not in z:
                 continue
