@@ -8,11 +8,12 @@ One step = the whole theta_h sweep (7 propagations).  Term-gate applications
 ("apps") = sum over rotation gates of the live terms entering the gate.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload kicked_ising|hubbard]
+                    [--workload kicked_ising|hubbard|hea]
 
 --workload hubbard measures the 6x6 Fermi-Hubbard Majorana propagation (144
 Majoranas, 10 Trotter steps, degree <= 6, tau = 1e-7) instead; one step = one
-propagation.
+propagation.  --workload hea measures 256 instances of a 50-qubit ansatz in one
+batched propagation plus the adjoint gradient of every angle.
 
 Prints one JSON line on rank 0.  Multi-GPU runs are independent replicas (the
 propagation of one observable does not shard without a per-gate exchange):
@@ -136,7 +137,58 @@ class Hubbard:
                 "mincoeff": 1e-7, "observable": "0.5 (1 + i g0 g1)"}
 
 
-WORKLOADS = {"kicked_ising": KickedIsing, "hubbard": Hubbard}
+class BatchedAnsatz:
+    """256 instances of a 50-qubit open-chain hardware-efficient ansatz (8 layers of
+    RY on every qubit then CZ on the bonds), per-instance angles from uniform[-pi, pi]
+    and per-instance observables of 1..64 random weight-1..4 terms, W = 6,
+    tau = 1e-7.  One step = one batched propagation of all 256 instances with
+    checkpoints, then the adjoint gradient d<O_i>/dtheta of all 400 angles of
+    every instance."""
+    name = "hea_50q_8layers_256inst_w6_tau1e-7"
+    metric = ("term-gate applications/s (256-instance 50-qubit ansatz, W=6, tau=1e-7; "
+              "forward + adjoint gradient per step)")
+    kind = "batched"
+    ninst, nq, layers = 256, 50, 8
+    cpu_instances = 16
+
+    def tables(self):
+        import fastfermion_gb300 as ff
+        from fastfermion_gb300 import workloads as W
+        self.thetas, self.obs = W.hea_instances(self.ninst, n=self.nq, layers=self.layers)
+        self.keys = np.concatenate([o[0] for o in self.obs], axis=1)
+        self.re = np.concatenate([o[1] for o in self.obs])
+        self.off = np.cumsum([0] + [o[1].size for o in self.obs]).astype(np.int64)
+        return [ff.encode_pauli_circuit(ff.build_circuit(W.hea_circuit(self.nq, self.layers)))]
+
+    def params(self):
+        return dict(maxdegree=6, topk=0, mincoeff=1e-7, max_xweight=-1, xtrunc_period=1, batched=1,
+                    deterministic=0)
+
+    def cpu_sample(self, tabs, cores, min_seconds=0.0):
+        """The oracle's sharded OpenMP port of the reference, instance by instance
+        (the reference has no batching), on the first cpu_instances instances."""
+        from oracle import oracle as O
+        tab = tabs[0]
+        apps = 0
+        t0 = time.perf_counter()
+        for i in range(self.cpu_instances):
+            t = tab.copy()
+            t["theta"][t["kind"] == 0] = self.thetas[i]
+            k, r = self.obs[i]
+            apps += O.pauli_propagate(t, k, r, np.zeros(r.size), maxdegree=6, mincoeff=1e-7,
+                                      n_threads=cores).apps
+        return apps, time.perf_counter() - t0, cores, (
+            f"the first {self.cpu_instances} of 256 instances, forward only, one at a time, sharded "
+            "OpenMP port of the reference algorithm (the reference has no gradient)")
+
+    def config(self):
+        return {"workload": self.name, "instances": self.ninst, "qubits": self.nq, "layers": self.layers,
+                "angles_per_instance": self.nq * self.layers, "maxdegree": 6, "mincoeff": 1e-7,
+                "observables": "1..64 random terms of weight 1..4, N(0,1) coefficients",
+                "checkpoint_every": 1}
+
+
+WORKLOADS = {"kicked_ising": KickedIsing, "hubbard": Hubbard, "hea": BatchedAnsatz}
 
 
 def parse():
@@ -292,6 +344,80 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+# GPU arm, batched ansatz (forward + adjoint through the public C ABI)
+# ---------------------------------------------------------------------------
+def main_batched(args, rank, ws, local, dist):
+    import torch
+
+    from fastfermion_gb300 import _native
+    torch.cuda.set_device(local)
+    ctx = _native.context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    wl = args.wl
+    tabs = wl.tables()
+    l2 = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    w = np.ones(wl.ninst)
+
+    def step():
+        expect, h = ctx.pauli_propagate_batched(wl.keys, wl.re, wl.off, tabs[0], wl.thetas, wl.params(), 1)
+        pr = ctx.profile()
+        t1 = time.perf_counter()
+        g, _ = h.adjoint(w)
+        t_adj = time.perf_counter() - t1
+        h.free()
+        return pr["apps"], pr["kernel_launches"], pr["seconds_total"], t_adj, expect, g
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(dist)
+    times, host_times, apps_tot, launches, fwd_s, adj_s = [], [], 0, 0, 0.0, 0.0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            l2.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            t0 = time.perf_counter()
+            e0.record(stream)
+            a, nl, tf, ta, _, _ = step()
+            e1.record(stream)
+            e1.synchronize()
+            host_times.append(time.perf_counter() - t0)
+            times.append(e0.elapsed_time(e1) * 1e-3)
+            apps_tot += a
+            launches += nl
+            fwd_s += tf
+            adj_s += ta
+    barrier(dist)
+    t_max = allmax(dist, sum(times))
+    value = allsum(dist, apps_tot) / t_max
+    e2e = allsum(dist, apps_tot) / allmax(dist, sum(host_times))
+    cpu = cpu_baseline(wl, tabs) if rank == 0 and not args.no_cpu_baseline else None
+    if rank == 0:
+        k = args.steps
+        h2d = wl.keys.nbytes + wl.re.nbytes + wl.off.nbytes + wl.thetas.nbytes + tabs[0].nbytes
+        d2h = wl.ninst * 8 + wl.thetas.nbytes
+        print(json.dumps({
+            "metric": wl.metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": k, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_max / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": dict(wl.config(), apps_per_step=apps_tot / k, forward_ms=1e3 * fwd_s / k,
+                           adjoint_ms=1e3 * adj_s / k, l2="flushed between steps (512 MB write)",
+                           parallelism=f"replicas{ws}",
+                           inputs="host arrays (the batched entry point copies them in each step)"),
+            "roofline": None,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+        }))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def main():
@@ -299,6 +425,8 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     rank, ws, local, dist = dist_init()
+    if args.wl.kind == "batched":
+        return main_batched(args, rank, ws, local, dist)
     import torch
 
     import fastfermion_gb300 as ff  # noqa: F401

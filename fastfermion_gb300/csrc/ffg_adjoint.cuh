@@ -179,7 +179,6 @@ __device__ bool adj_group(const StoreView& in, const OrbitScratch& sc, const Adj
             const BatchGate G = a.gates[t];
             double gc, gs;
             gate_cs(a, G, t, inst, gc, gs);
-            const cplx isin = {0.0, gs};
             const u32 cnt0 = *(volatile u32*)T.cnt;
             for (u32 m = rank; m < cnt0; m += TEAM) T.hist[(u64)m * na + ti] = T.c[m];
             team_sync<TEAM>();
@@ -207,15 +206,15 @@ __device__ bool adj_group(const StoreView& in, const OrbitScratch& sc, const Adj
                 if (j >= 0 && (u32)j < cnt0) {
                     if ((u32)j < m) continue;  // the pair belongs to member j
                     const cplx cj = {T.c[j], 0.0};
-                    cplx ni = cscale(ci, gc), nj = cscale(cj, gc);
-                    if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
-                    if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
+                    cplx ni = rot_keep<false>(ci, gc), nj = rot_keep<false>(cj, gc);
+                    if (dQ <= a.maxdeg) ni = rot_add<false>(ni, rot_partner<false>(cj, gs, jK));
+                    if (dK <= a.maxdeg) nj = rot_add<false>(nj, rot_partner<false>(ci, gs, jQ));
                     T.c[m] = ni.re;
                     T.c[j] = nj.re;
                 } else {
-                    T.c[m] = cscale(ci, gc).re;
+                    T.c[m] = rot_keep<false>(ci, gc).re;
                     if (dK <= a.maxdeg) {
-                        const cplx nv = cadd({0.0, 0.0}, cmul(cmul(ci, isin), ipow(jQ)));
+                        const cplx nv = rot_add<false>({0.0, 0.0}, rot_partner<false>(ci, gs, jQ));
                         const u32 idx = atomicAdd(T.cnt, 1u);
                         if (idx >= T.cap) {
                             atomicExch(T.flag, 1u);

@@ -170,6 +170,40 @@ __device__ __forceinline__ cplx ipow(int m) {
     }
 }
 
+// Rotation update terms with a real-mode specialisation.  With imaginary parts
+// zero, the complex expressions of the reference reduce exactly (same IEEE
+// result up to the sign of zero) to:
+//   keep:    (a, 0) * c                          -> a*c
+//   partner: (b, 0) * (0, s) * i^j               -> -(b*s) for j = 1 mod 4,
+//                                                   +(b*s) for j = 3 mod 4,
+//                                                   (+-)0 for even j
+//   sum:     x + y                               -> one rounding of the real parts
+// (the partner product is b*s + 0 then a sign flip, both exact).  Real mode is
+// used only for finite inputs: with an infinite coefficient the complex form
+// produces NaN where the reduced form would not.
+template <bool CPLX>
+__device__ __forceinline__ cplx rot_keep(cplx a, double c) {
+    if (CPLX) return cscale(a, c);
+    return {__dmul_rn(a.re, c), 0.0};
+}
+
+template <bool CPLX>
+__device__ __forceinline__ cplx rot_partner(cplx b, double s, int j) {
+    if (CPLX) return cmul(cmul(b, {0.0, s}), ipow(j));
+    const double p = __dmul_rn(b.re, s);
+    switch (j & 3) {
+        case 1: return {-p, 0.0};
+        case 3: return {p, 0.0};
+        default: return {0.0, 0.0};
+    }
+}
+
+template <bool CPLX>
+__device__ __forceinline__ cplx rot_add(cplx a, cplx b) {
+    if (CPLX) return cadd(a, b);
+    return {__dadd_rn(a.re, b.re), 0.0};
+}
+
 // ---------------------------------------------------------------------------
 // Truncation predicate |c| <= tau with |c| = hypot(re, im) correctly rounded
 // (the reference uses std::abs on std::complex<double>, i.e. libm hypot).

@@ -171,7 +171,8 @@ struct ffg_ctx {
     size_t groups2_cap = 0;
     bool orbit = true;          // batch-orbit path for long commuting runs (FFG_ORBIT=0 disables)
     int orbit_min_gates = 4;    // shortest run sent to the batch-orbit path
-    int orbit_route_big = 10;   // |A| from which a group skips the warp-level pass (FFG_ORBIT_ROUTE)
+    int orbit_route_big = 8;    // |A| from which a group skips the warp-level pass (FFG_ORBIT_ROUTE)
+    bool orbit_team = true;     // 256-thread team pass before the 1024-thread pass (FFG_ORBIT_TEAM=0 disables)
     BatchGate* d_bgates = nullptr;
     size_t bgates_cap = 0;
     char* d_oscratch = nullptr;
@@ -814,21 +815,31 @@ struct Engine {
         constexpr int NWo = PAULI ? NW : 1;
         u32* list = sc.big;
         u32* other = retry_list;
-        bool smem_pass = true;  // first a shared-memory table per block, then global regions
+        // passes: 0 = 256-thread teams with kTeamCap-member shared-memory tables
+        // (several blocks per SM), 1 = 1024-thread blocks with kBlockCap-member
+        // tables, 2+ = 1024-thread blocks with global-memory regions (x4 each pass)
+        int pass = ctx->orbit_team ? 0 : 1;
         u64 rcap = 1ull << 14;
         const size_t tb = block_table_bytes<KW, CPLX>();
+        const size_t tt = block_table_bytes<KW, CPLX, kTeamCap>();
         static bool attr_set = false;
+        static int team_per_sm = 1;
         if (!attr_set) {
             CK(cudaFuncSetAttribute(orbit_process_big<NWo, CPLX, true>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb));
+            CK(cudaFuncSetAttribute(orbit_process_big<NWo, CPLX, true, 256, kTeamCap>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tt));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &team_per_sm, orbit_process_big<NWo, CPLX, true, 256, kTeamCap>, 256, tt));
+            team_per_sm = std::max(team_per_sm, 1);
             attr_set = true;
         }
         while (nbig > 0) {
-            const u32 grid = std::min<u32>(nbig, (u32)ctx->num_sms);
+            const u32 grid = std::min<u32>(nbig, (u32)ctx->num_sms * (pass == 0 ? (u32)team_per_sm : 1u));
             BigPool bp{};
             bp.retry = other;
             bp.nretry = nretry;
-            if (!smem_pass) {
+            if (pass >= 2) {
                 const u64 region =
                     align256((size_t)KW * rcap * 8 + rcap * 8 * (CPLX ? 2 : 1) + 2 * rcap * 4 + 8);
                 int rc = ensure_buf(ctx, ctx->bigpool, region * grid);
@@ -840,7 +851,10 @@ struct Engine {
             CK(cudaMemsetAsync(nretry, 0, 4, ctx->stream));
             {
                 PhaseScope ps(ctx, PH_ROT);
-                if (smem_pass)
+                if (pass == 0)
+                    orbit_process_big<NWo, CPLX, true, 256, kTeamCap><<<grid, 256, tt, ctx->stream>>>(
+                        cur.v, out, sc, ctx->d_oc, a, bp, list, nbig);
+                else if (pass == 1)
                     orbit_process_big<NWo, CPLX, true><<<grid, 1024, tb, ctx->stream>>>(cur.v, out, sc, ctx->d_oc,
                                                                                       a, bp, list, nbig);
                 else
@@ -862,8 +876,8 @@ struct Engine {
             if (hr == 0) return 0;
             std::swap(list, other);
             nbig = hr;
-            if (!smem_pass) rcap *= 4;
-            smem_pass = false;
+            if (pass >= 2) rcap *= 4;
+            pass++;
             if (rcap > (1ull << 26)) return set_err(ctx, FFG_ERR_STATE, "orbit group larger than 2^26 terms");
         }
         return 0;
@@ -1782,6 +1796,7 @@ int ffg_create(ffg_ctx** out, int device) {
     if (const char* d = getenv("FFG_ORBIT")) ctx->orbit = atoi(d) != 0;
     if (const char* d = getenv("FFG_ORBIT_MIN")) ctx->orbit_min_gates = std::max(1, atoi(d));
     if (const char* d = getenv("FFG_ORBIT_ROUTE")) ctx->orbit_route_big = std::max(1, atoi(d));
+    if (const char* d = getenv("FFG_ORBIT_TEAM")) ctx->orbit_team = atoi(d) != 0;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -1870,27 +1885,28 @@ int ffg_pauli_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, co
                 if (G.q0 >= 64 || (two && G.q1 >= 64)) wide = true;
             }
         }
+        // complex mode when some coefficient has an imaginary part, or is not
+        // finite (the real-mode reduction of the update holds for finite values)
         bool cplx = false;
         std::vector<uint64_t> hk;
         if (!on_device) {
             for (size_t i = 0; i < n && !wide; i++)
                 if (keys[n + i] || keys[3 * n + i]) wide = true;
-            if (im)
-                for (size_t i = 0; i < n && !cplx; i++)
-                    if (im[i] != 0.0) cplx = true;
+            for (size_t i = 0; i < n && !cplx; i++)
+                if (!std::isfinite(re[i]) || (im && im[i] != 0.0)) cplx = true;
         } else {
             // device input: inspect on the host (one copy of the key planes)
             hk.resize(4 * n);
-            std::vector<double> him(n);
+            std::vector<double> hre(n), him(n);
             if (n) {
                 CK(cudaMemcpy(hk.data(), keys, 4 * n * 8, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpy(hre.data(), re, n * 8, cudaMemcpyDeviceToHost));
                 if (im) CK(cudaMemcpy(him.data(), im, n * 8, cudaMemcpyDeviceToHost));
             }
             for (size_t i = 0; i < n && !wide; i++)
                 if (hk[n + i] || hk[3 * n + i]) wide = true;
-            if (im)
-                for (size_t i = 0; i < n && !cplx; i++)
-                    if (him[i] != 0.0) cplx = true;
+            for (size_t i = 0; i < n && !cplx; i++)
+                if (!std::isfinite(hre[i]) || (im && him[i] != 0.0)) cplx = true;
         }
         const int nw = wide ? 2 : 1;
         std::vector<Op> ops;
@@ -2271,6 +2287,8 @@ int ffg_pauli_propagate_batched(ffg_ctx* ctx, const uint64_t* keys, const double
     if (bp->checkpoint_every < 0) return set_err(ctx, FFG_ERR_ARG, "checkpoint_every must be >= 0");
     if (ctx->group_d != 1 || !ctx->orbit || !ctx->persistent)
         return set_err(ctx, FFG_ERR_ARG, "batched propagation needs the orbit and persistent paths (FFG_* overrides)");
+    for (size_t i = 0; i < n; i++)
+        if (!std::isfinite(re[i])) return set_err(ctx, FFG_ERR_ARG, "batched propagation needs finite coefficients");
     try {
         auto t0 = std::chrono::steady_clock::now();
         reset_profile(ctx);

@@ -119,7 +119,7 @@ __device__ __forceinline__ void store_coef(const StoreView& s, u64 i, cplx v) {
 template <int KW, bool CPLX>
 __device__ __forceinline__ int emit_partner(const StoreView& s, DevCounters* C, u64 n_in,
                                             long long dead_slot, const u64 (&k)[KW], cplx v) {
-    const cplx nv = cadd({0.0, 0.0}, v);  // operator[] starts from complex zero
+    const cplx nv = rot_add<CPLX>({0.0, 0.0}, v);  // operator[] starts from complex zero
     const u64 pos = n_in + atomicAdd(&C->d_app, 1ull);
 #pragma unroll
     for (int w = 0; w < KW; w++) s.key[(u64)w * s.cap + pos] = k[w];
@@ -182,17 +182,17 @@ __global__ void __launch_bounds__(kBlock) pauli_rot_kernel(StoreView s, DevCount
             if (j >= 0 && !s.dead[j]) {
                 if ((u64)j < i) continue;  // the pair belongs to position j
                 const cplx cj = load_coef<CPLX>(s, (u64)j);
-                cplx ni = cscale(ci, a.c), nj = cscale(cj, a.c);
-                if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
-                if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
+                cplx ni = rot_keep<CPLX>(ci, a.c), nj = rot_keep<CPLX>(cj, a.c);
+                if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, isin.im, jK));
+                if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, isin.im, jQ));
                 emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
                 store_coef<CPLX>(s, i, ni);
                 store_coef<CPLX>(s, (u64)j, nj);
             } else {
-                store_coef<CPLX>(s, i, cscale(ci, a.c));
+                store_coef<CPLX>(s, i, rot_keep<CPLX>(ci, a.c));
                 if (dK <= a.maxdeg) {
                     d_alive += emit_partner<KW, CPLX>(s, C, n_in, j >= 0 ? (long long)js : -1, k,
-                                                      cmul(cmul(ci, isin), ipow(jQ)));
+                                                      rot_partner<CPLX>(ci, isin.im, jQ));
                     emits++;
                 }
             }
@@ -794,10 +794,10 @@ __device__ __forceinline__ void group_orbit(const StoreView& s, DevCounters* C, 
             const bool to_u = pv && du <= a.maxdeg;
             const bool to_v = pu && dv <= a.maxdeg;
             cplx nu = c[u], nv = c[v];
-            if (pu) nu = cscale(c[u], a.c[t]);
-            if (pv) nv = cscale(c[v], a.c[t]);
-            if (to_u) nu = cadd(pu ? nu : cplx{0.0, 0.0}, cmul(cmul(c[v], isin), ipow(jv)));
-            if (to_v) nv = cadd(pv ? nv : cplx{0.0, 0.0}, cmul(cmul(c[u], isin), ipow(ju)));
+            if (pu) nu = rot_keep<CPLX>(c[u], a.c[t]);
+            if (pv) nv = rot_keep<CPLX>(c[v], a.c[t]);
+            if (to_u) nu = rot_add<CPLX>(pu ? nu : cplx{0.0, 0.0}, rot_partner<CPLX>(c[v], isin.im, jv));
+            if (to_v) nv = rot_add<CPLX>(pv ? nv : cplx{0.0, 0.0}, rot_partner<CPLX>(c[u], isin.im, ju));
             emits += (int)to_u + (int)to_v;
             if (!pu && to_u) {
                 present |= 1u << u;
@@ -1051,17 +1051,17 @@ __global__ void __launch_bounds__(kBlock, 5) pauli_pair_kernel(StoreView s, DevC
             const cplx isin = {0.0, a.s};
             if (j >= 0 && !jdead) {
                 if ((u64)j < i) continue;  // the pair belongs to position j
-                cplx ni = cscale(ci, a.c), nj = cscale(cj, a.c);
-                if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
-                if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
+                cplx ni = rot_keep<CPLX>(ci, a.c), nj = rot_keep<CPLX>(cj, a.c);
+                if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, isin.im, jK));
+                if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, isin.im, jQ));
                 emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
                 store_coef<CPLX>(s, i, ni);
                 store_coef<CPLX>(s, (u64)j, nj);
             } else {
-                store_coef<CPLX>(s, i, cscale(ci, a.c));
+                store_coef<CPLX>(s, i, rot_keep<CPLX>(ci, a.c));
                 if (dK <= a.maxdeg) {
                     d_alive += emit_partner<KW, CPLX>(s, C, n_in, j >= 0 ? (long long)jslot : -1, k,
-                                                      cmul(cmul(ci, isin), ipow(jQ)));
+                                                      rot_partner<CPLX>(ci, isin.im, jQ));
                     emits++;
                 }
             }

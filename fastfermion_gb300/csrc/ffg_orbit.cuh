@@ -420,7 +420,6 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                 u64 P[KW];
 #pragma unroll
                 for (int w = 0; w < KW; w++) P[w] = G.p[w];
-                const cplx isin = {0.0, gs};
                 const int cnt0 = (int)*(volatile unsigned int*)&T.cnt;
                 __syncwarp();
                 for (int m = lane; m < cnt0; m += 32) {
@@ -447,9 +446,9 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                     if (j >= 0 && j < cnt0) {
                         if (j < m) continue;  // the pair belongs to member j
                         const cplx cj = {T.re[j], CPLX ? T.im[j] : 0.0};
-                        cplx ni = cscale(ci, gc), nj = cscale(cj, gc);
-                        if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
-                        if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
+                        cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
+                        if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
+                        if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
                         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
                         T.re[m] = ni.re;
                         T.re[j] = nj.re;
@@ -458,12 +457,12 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                             T.im[j] = nj.im;
                         }
                     } else {
-                        const cplx ni = cscale(ci, gc);
+                        const cplx ni = rot_keep<CPLX>(ci, gc);
                         T.re[m] = ni.re;
                         if (CPLX) T.im[m] = ni.im;
                         if (dK <= a.maxdeg) {
                             g_emits++;
-                            const cplx nv = cadd({0.0, 0.0}, cmul(cmul(ci, isin), ipow(jQ)));
+                            const cplx nv = rot_add<CPLX>({0.0, 0.0}, rot_partner<CPLX>(ci, gs, jQ));
                             const unsigned int idx = atomicAdd(&T.cnt, 1u);
                             if (idx >= (unsigned int)kOrbitCap) {
                                 atomicExch(&T.flag, 1u);
@@ -598,16 +597,18 @@ __device__ __forceinline__ void big_insert(const BigRegion<KW, CPLX>& G, u32 rca
 }
 
 constexpr u32 kBlockCap = 4096;  // members of a block-level table held in shared memory
+constexpr u32 kTeamCap = 1024;   // members of a team-level table (256-thread blocks, several per SM)
 
-template <int KW, bool CPLX>
+template <int KW, bool CPLX, u32 CAP = kBlockCap>
 constexpr size_t block_table_bytes() {
-    return (size_t)KW * kBlockCap * 8 + kBlockCap * 8 * (CPLX ? 2 : 1) + 2 * kBlockCap * 4 + 16;
+    return (size_t)KW * CAP * 8 + CAP * 8 * (CPLX ? 2 : 1) + 2 * CAP * 4 + 16;
 }
 
-// Block-level group processing.  SM: the table lives in dynamic shared memory
-// (kBlockCap members); otherwise in the block's global-memory region of bp.
-template <int NW, bool CPLX, bool SM>
-__global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreView out, OrbitScratch sc,
+// Block-level group processing with TB threads per block.  SM: the table lives
+// in dynamic shared memory (CAP members); otherwise in the block's
+// global-memory region of bp.
+template <int NW, bool CPLX, bool SM, int TB = 1024, u32 CAP = kBlockCap>
+__global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView out, OrbitScratch sc,
                                                           OrbitCounters* oc, OrbitBatchArgs a, BigPool bp,
                                                           const u32* list, u32 nlist) {
     constexpr int KW = 2 * NW;
@@ -621,16 +622,16 @@ __global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreVie
         BigRegion<KW, CPLX> G;
         u32 rcap;
         if (SM) {
-            rcap = kBlockCap;
+            rcap = CAP;
             char* p = (char*)btab;
             G.key = (u64*)p;
-            p += (size_t)KW * kBlockCap * 8;
+            p += (size_t)KW * CAP * 8;
             G.re = (double*)p;
-            p += kBlockCap * 8;
+            p += CAP * 8;
             G.im = (double*)p;
-            if (CPLX) p += kBlockCap * 8;
+            if (CPLX) p += CAP * 8;
             G.slot = (u32*)p;
-            p += 2 * kBlockCap * 4;
+            p += 2 * CAP * 4;
             G.cnt = (u32*)p;
             G.flag = G.cnt + 1;
         } else {
@@ -681,7 +682,6 @@ __global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreVie
                 u64 P[KW];
 #pragma unroll
                 for (int w = 0; w < KW; w++) P[w] = Gt.p[w];
-                const cplx isin = {0.0, gs};
                 const u32 cnt0 = *(volatile u32*)G.cnt;
                 __syncthreads();
                 for (u32 m = threadIdx.x; m < cnt0; m += blockDim.x) {
@@ -711,9 +711,9 @@ __global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreVie
                     if (j >= 0 && (u32)j < cnt0) {
                         if ((u32)j < m) continue;
                         const cplx cj = {tld<SM>(&G.re[j]), CPLX ? tld<SM>(&G.im[j]) : 0.0};
-                        cplx ni = cscale(ci, gc), nj = cscale(cj, gc);
-                        if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
-                        if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
+                        cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
+                        if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
+                        if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
                         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
                         G.re[m] = ni.re;
                         G.re[j] = nj.re;
@@ -722,12 +722,12 @@ __global__ void __launch_bounds__(1024) orbit_process_big(StoreView in, StoreVie
                             G.im[j] = nj.im;
                         }
                     } else {
-                        const cplx ni = cscale(ci, gc);
+                        const cplx ni = rot_keep<CPLX>(ci, gc);
                         G.re[m] = ni.re;
                         if (CPLX) G.im[m] = ni.im;
                         if (dK <= a.maxdeg) {
                             g_emits++;
-                            const cplx nv = cadd({0.0, 0.0}, cmul(cmul(ci, isin), ipow(jQ)));
+                            const cplx nv = rot_add<CPLX>({0.0, 0.0}, rot_partner<CPLX>(ci, gs, jQ));
                             const u32 idx = atomicAdd(G.cnt, 1u);
                             if (idx >= rcap) {
                                 atomicExch(G.flag, 1u);

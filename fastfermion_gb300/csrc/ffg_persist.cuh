@@ -172,16 +172,16 @@ __device__ __forceinline__ void pair_one(const StoreView& s, DevCounters* C, u64
     const cplx isin = {0.0, a.s};
     if (j >= 0 && !jdead) {
         if ((u64)j < i) return;  // the pair belongs to position j
-        cplx ni = cscale(ci, a.c), nj = cscale(cj, a.c);
-        if (dQ <= a.maxdeg) ni = cadd(ni, cmul(cmul(cj, isin), ipow(jK)));
-        if (dK <= a.maxdeg) nj = cadd(nj, cmul(cmul(ci, isin), ipow(jQ)));
+        cplx ni = rot_keep<CPLX>(ci, a.c), nj = rot_keep<CPLX>(cj, a.c);
+        if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, isin.im, jK));
+        if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, isin.im, jQ));
         emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
         store_coef<CPLX>(s, i, ni);
         store_coef<CPLX>(s, (u64)j, nj);
     } else {
-        store_coef<CPLX>(s, i, cscale(ci, a.c));
+        store_coef<CPLX>(s, i, rot_keep<CPLX>(ci, a.c));
         if (dK <= a.maxdeg) {
-            const cplx nv = cadd({0.0, 0.0}, cmul(cmul(ci, isin), ipow(jQ)));
+            const cplx nv = rot_add<CPLX>({0.0, 0.0}, rot_partner<CPLX>(ci, isin.im, jQ));
             const u64 p = n_in + atomicAdd(app_ctr, 1ull);
 #pragma unroll
             for (int w = 0; w < KW; w++) s.key[(u64)w * s.cap + p] = k[w];
