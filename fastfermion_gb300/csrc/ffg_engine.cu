@@ -809,17 +809,15 @@ struct Engine {
     u32* retry_list = nullptr;
     u32* nretry = nullptr;
 
-    // Block-level pass over the groups in `list`; returns 0 when every group
-    // fit, 2 when the output store overflowed, else a negative status.
-    int exec_big_groups(const StoreView& out, OrbitScratch& sc, const OrbitBatchArgs& a, u32 nbig) {
+    // Big-group tiers.  launch_big_tiers enqueues the shared-memory passes right
+    // after the warp pass, reading the list lengths on the device (no host
+    // round trip): 256-thread teams with kTeamCap-member tables (several blocks
+    // per SM), then 1024-thread blocks with kBlockCap-member tables over the
+    // team pass's overflow.  Groups left after both (more than kBlockCap
+    // members) are listed in sc.big with their count in nretry[1];
+    // finish_big_groups runs them with global-memory regions (x4 per pass).
+    int launch_big_tiers(const StoreView& out, OrbitScratch& sc, const OrbitBatchArgs& a) {
         constexpr int NWo = PAULI ? NW : 1;
-        u32* list = sc.big;
-        u32* other = retry_list;
-        // passes: 0 = 256-thread teams with kTeamCap-member shared-memory tables
-        // (several blocks per SM), 1 = 1024-thread blocks with kBlockCap-member
-        // tables, 2+ = 1024-thread blocks with global-memory regions (x4 each pass)
-        int pass = ctx->orbit_team ? 0 : 1;
-        u64 rcap = 1ull << 14;
         const size_t tb = block_table_bytes<KW, CPLX>();
         const size_t tt = block_table_bytes<KW, CPLX, kTeamCap>();
         static bool attr_set = false;
@@ -834,32 +832,56 @@ struct Engine {
             team_per_sm = std::max(team_per_sm, 1);
             attr_set = true;
         }
-        while (nbig > 0) {
-            const u32 grid = std::min<u32>(nbig, (u32)ctx->num_sms * (pass == 0 ? (u32)team_per_sm : 1u));
+        BigPool bp{};
+        const u32* nbig_dev = &ctx->d_oc->nbig;
+        PhaseScope ps(ctx, PH_ROT);
+        if (ctx->orbit_team) {
+            // sc.big -> retry_list (count nretry[0]) -> sc.big (count nretry[1])
+            bp.retry = retry_list;
+            bp.nretry = nretry;
+            orbit_process_big<NWo, CPLX, true, 256, kTeamCap><<<ctx->num_sms * team_per_sm, 256, tt, ctx->stream>>>(
+                cur.v, out, sc, ctx->d_oc, a, bp, sc.big, 0, nbig_dev);
+            bp.retry = sc.big;
+            bp.nretry = nretry + 1;
+            orbit_process_big<NWo, CPLX, true><<<ctx->num_sms, 1024, tb, ctx->stream>>>(
+                cur.v, out, sc, ctx->d_oc, a, bp, retry_list, 0, nretry);
+            ctx->prof.kernel_launches += 2;
+        } else {
+            // sc.big -> retry_list (count nretry[1])
+            bp.retry = retry_list;
+            bp.nretry = nretry + 1;
+            orbit_process_big<NWo, CPLX, true><<<ctx->num_sms, 1024, tb, ctx->stream>>>(
+                cur.v, out, sc, ctx->d_oc, a, bp, sc.big, 0, nbig_dev);
+            ctx->prof.kernel_launches++;
+        }
+        OSTEP("orbit_process_big");
+        return FFG_OK;
+    }
+
+    // Global-memory passes over the nleft groups left by launch_big_tiers;
+    // returns 0 when every group fit, 2 when the output store overflowed, else
+    // a negative status.
+    int finish_big_groups(const StoreView& out, OrbitScratch& sc, const OrbitBatchArgs& a, u32 nleft) {
+        constexpr int NWo = PAULI ? NW : 1;
+        u32* list = ctx->orbit_team ? sc.big : retry_list;
+        u32* other = ctx->orbit_team ? retry_list : sc.big;
+        u64 rcap = 1ull << 14;
+        while (nleft > 0) {
+            const u32 grid = std::min<u32>(nleft, (u32)ctx->num_sms);
             BigPool bp{};
             bp.retry = other;
             bp.nretry = nretry;
-            if (pass >= 2) {
-                const u64 region =
-                    align256((size_t)KW * rcap * 8 + rcap * 8 * (CPLX ? 2 : 1) + 2 * rcap * 4 + 8);
-                int rc = ensure_buf(ctx, ctx->bigpool, region * grid);
-                if (rc) return rc;
-                bp.base = ctx->bigpool.p;
-                bp.region_bytes = region;
-                bp.rcap = (u32)rcap;
-            }
+            const u64 region = align256((size_t)KW * rcap * 8 + rcap * 8 * (CPLX ? 2 : 1) + 2 * rcap * 4 + 8);
+            int rc = ensure_buf(ctx, ctx->bigpool, region * grid);
+            if (rc) return rc;
+            bp.base = ctx->bigpool.p;
+            bp.region_bytes = region;
+            bp.rcap = (u32)rcap;
             CK(cudaMemsetAsync(nretry, 0, 4, ctx->stream));
             {
                 PhaseScope ps(ctx, PH_ROT);
-                if (pass == 0)
-                    orbit_process_big<NWo, CPLX, true, 256, kTeamCap><<<grid, 256, tt, ctx->stream>>>(
-                        cur.v, out, sc, ctx->d_oc, a, bp, list, nbig);
-                else if (pass == 1)
-                    orbit_process_big<NWo, CPLX, true><<<grid, 1024, tb, ctx->stream>>>(cur.v, out, sc, ctx->d_oc,
-                                                                                      a, bp, list, nbig);
-                else
-                    orbit_process_big<NWo, CPLX, false><<<grid, 1024, 0, ctx->stream>>>(cur.v, out, sc, ctx->d_oc,
-                                                                                       a, bp, list, nbig);
+                orbit_process_big<NWo, CPLX, false><<<grid, 1024, 0, ctx->stream>>>(cur.v, out, sc, ctx->d_oc, a, bp,
+                                                                                   list, nleft, nullptr);
                 OSTEP("orbit_process_big");
                 ctx->prof.kernel_launches++;
             }
@@ -875,9 +897,8 @@ struct Engine {
             if (ctx->h_oc->overflow & 1u) return 2;
             if (hr == 0) return 0;
             std::swap(list, other);
-            nbig = hr;
-            if (pass >= 2) rcap *= 4;
-            pass++;
+            nleft = hr;
+            rcap *= 4;
             if (rcap > (1ull << 26)) return set_err(ctx, FFG_ERR_STATE, "orbit group larger than 2^26 terms");
         }
         return 0;
@@ -961,11 +982,11 @@ struct Engine {
             int rc = ensure_buf(ctx, ctx->buf[1 - active], store_bytes(KW, CPLX, out_cap));
             if (rc) return rc;
             Store dst = carve(ctx->buf[1 - active], KW, CPLX, out_cap);
-            CK(cudaMemsetAsync(ctx->d_oc, 0, sizeof(OrbitCounters), ctx->stream));
-            CK(cudaMemsetAsync(sc.gslots, 0xff, (sc.gmask + 1) * 8, ctx->stream));
             {
                 PhaseScope ps(ctx, PH_ROT);
                 const int g = grid_for(ctx, n_in);
+                orbit_init<<<grid_for(ctx, sc.gmask + 1), kBlock, 0, ctx->stream>>>(ctx->d_oc, sc.gslots,
+                                                                                  sc.gmask + 1, nretry);
                 orbit_classify<NWo, CPLX><<<g, kBlock, 0, ctx->stream>>>(cur.v, n_in, dst.v, sc, ctx->d_oc, a);
                 OSTEP("orbit_classify");
                 orbit_group<KW><<<g, kBlock, 0, ctx->stream>>>(n_in, sc, ctx->d_oc);
@@ -977,10 +998,14 @@ struct Engine {
                 orbit_process<NWo, CPLX><<<ctx->num_sms * 2, 32 * kOrbitWarps, smem, ctx->stream>>>(
                     cur.v, dst.v, sc, ctx->d_oc, a);
                 OSTEP("orbit_process");
-                ctx->prof.kernel_launches += 5;
+                ctx->prof.kernel_launches += 6;
             }
+            int rcb = launch_big_tiers(dst.v, sc, a);
+            if (rcb) return rcb;
             CK(cudaGetLastError());
+            u32 nleft = 0;
             CK(cudaMemcpyAsync(ctx->h_oc, ctx->d_oc, sizeof(OrbitCounters), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(&nleft, nretry + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaStreamSynchronize(ctx->stream));
             ctx->prof.syncs++;
             if (ctx->profiling) drain_events(ctx);
@@ -994,16 +1019,16 @@ struct Engine {
                 out_cap = pow2_at_least(oc.n_out + oc.n_out / 4 + 1024);
                 continue;
             }
-            if (oc.nbig) {
-                const int br = exec_big_groups(dst.v, sc, a, oc.nbig);
+            if (oc.chk_code == 0 && !(oc.overflow & 1u) && nleft) {
+                const int br = finish_big_groups(dst.v, sc, a, nleft);
                 if (br < 0) return br;
                 oc = *ctx->h_oc;
                 if (br == 2) {
                     out_cap = pow2_at_least(oc.n_out + oc.n_out / 4 + 1024);
                     continue;
                 }
-                ctx->prof.orbit_fallbacks += oc.nbig;  // groups done by the block-level pass
             }
+            ctx->prof.orbit_fallbacks += oc.nbig;  // groups done by the block-level passes
             ctx->prof.orbit_max_group = std::max<int64_t>(ctx->prof.orbit_max_group, oc.max_members);
             ctx->prof.orbit_batches++;
             ctx->prof.orbit_groups += oc.ngroups;
@@ -1153,9 +1178,7 @@ struct Engine {
             if (!rc) rc = sync_counters();
             return rc;
         }
-        int rc = sync_counters();
-        if (rc) return rc;
-        rc = exec_orbit_batch(r.g0, r.k, r.has_trunc ? &r.trunc : nullptr, maxdeg);
+        int rc = exec_orbit_batch(r.g0, r.k, r.has_trunc ? &r.trunc : nullptr, maxdeg);
         if (rc == 1) return set_err(ctx, FFG_ERR_STATE, "batched propagation: orbit group larger than 2^26 terms");
         return rc;
     }
@@ -1180,8 +1203,8 @@ struct Engine {
                 rc = exec_persistent(pos, b.first);
                 if (rc) return rc;
             }
-            rc = sync_counters();
-            if (rc) return rc;
+            // the host counters are current here: the persistent run and the
+            // orbit batch both leave them up to date
             if (ctx->h_ctr->n != ctx->h_ctr->alive) {
                 rc = compact_into(1 - active, cap);  // the orbit path reads a dense store
                 if (rc) return rc;
@@ -1690,7 +1713,7 @@ int batch_adjoint(ffg_batch* h, const double* weights, double* grad_theta, doubl
             a.thr = rec.has_trunc ? rec.trunc.thr : 0;
             a.tau = rec.has_trunc ? rec.trunc.tau : 0.0;
             a.max_xweight = rec.has_trunc ? rec.trunc.max_xweight : -1;
-            a.route_big = ctx->orbit_route_big;
+            a.route_big = (int)kAdjWarpGates + 1;  // the warp tier takes every group its tables hold
             a.inst_cs = h->bc.d_inst_cs + (size_t)rec.g0 * ninst;
             a.ninst = (u32)ninst;
             a.inst_plane = h->bc.inst_plane;

@@ -156,6 +156,16 @@ __device__ __forceinline__ void out_append(const StoreView& o, OrbitCounters* oc
     o.dead[pos] = 0;
 }
 
+// Per-batch reset: counters, the group index and the two retry counts.
+__global__ void __launch_bounds__(kBlock) orbit_init(OrbitCounters* oc, u64* gslots, u64 nslots, u32* nretry) {
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    const u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    for (u64 i = t; i < nslots; i += stride) gslots[i] = ~0ull;
+    constexpr u32 nw = sizeof(OrbitCounters) / 4;
+    for (u64 i = t; i < nw; i += stride) ((u32*)oc)[i] = 0;
+    if (t < 2) nretry[t] = 0;
+}
+
 // A(Q) for every input term; group key; final terms go to the output.
 template <int NW, bool CPLX>
 __global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, u64 n_in, StoreView out,
@@ -610,10 +620,11 @@ constexpr size_t block_table_bytes() {
 template <int NW, bool CPLX, bool SM, int TB = 1024, u32 CAP = kBlockCap>
 __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView out, OrbitScratch sc,
                                                           OrbitCounters* oc, OrbitBatchArgs a, BigPool bp,
-                                                          const u32* list, u32 nlist) {
+                                                          const u32* list, u32 nlist, const u32* nlist_dev) {
     constexpr int KW = 2 * NW;
     __shared__ long long red[3][32];
     extern __shared__ __align__(16) unsigned char btab[];
+    if (nlist_dev) nlist = *(volatile const u32*)nlist_dev;  // list length written by an earlier kernel
     long long emits = 0, created = 0, xapps = 0;
     for (u32 gi = blockIdx.x; gi < nlist; gi += gridDim.x) {
         OCHK(gi < sc.cap_in, 8, gi, nlist, 0)
