@@ -179,6 +179,8 @@ struct ffg_ctx {
     size_t oscratch_bytes = 0;
     OrbitCounters* d_oc = nullptr;
     OrbitCounters* h_oc = nullptr;  // pinned
+    OrbitCounters* d_ocw = nullptr;  // counters of a window of orbit batches (kOrbitWindow)
+    OrbitCounters* h_ocw = nullptr;  // pinned
     RawBuf bigpool;                 // global-memory tables of large orbit groups
     const BatchCtx* batch = nullptr;  // set while a batched propagation runs
     ffg_profile prof{};
@@ -227,6 +229,7 @@ struct ffg_batch {
 namespace {
 
 constexpr int kMaxParts = 1024;
+constexpr int kOrbitWindow = 16;  // orbit batches enqueued per host round trip
 constexpr int kChunkOps = 128;
 
 #define CK(call)                                                                          \
@@ -816,7 +819,8 @@ struct Engine {
     // team pass's overflow.  Groups left after both (more than kBlockCap
     // members) are listed in sc.big with their count in nretry[1];
     // finish_big_groups runs them with global-memory regions (x4 per pass).
-    int launch_big_tiers(const StoreView& out, OrbitScratch& sc, const OrbitBatchArgs& a) {
+    int launch_big_tiers(const StoreView& in, const StoreView& out, OrbitScratch& sc, const OrbitBatchArgs& a,
+                         OrbitCounters* oc) {
         constexpr int NWo = PAULI ? NW : 1;
         const size_t tb = block_table_bytes<KW, CPLX>();
         const size_t tt = block_table_bytes<KW, CPLX, kTeamCap>();
@@ -833,25 +837,25 @@ struct Engine {
             attr_set = true;
         }
         BigPool bp{};
-        const u32* nbig_dev = &ctx->d_oc->nbig;
+        const u32* nbig_dev = &oc->nbig;
         PhaseScope ps(ctx, PH_ROT);
         if (ctx->orbit_team) {
             // sc.big -> retry_list (count nretry[0]) -> sc.big (count nretry[1])
             bp.retry = retry_list;
             bp.nretry = nretry;
             orbit_process_big<NWo, CPLX, true, 256, kTeamCap><<<ctx->num_sms * team_per_sm, 256, tt, ctx->stream>>>(
-                cur.v, out, sc, ctx->d_oc, a, bp, sc.big, 0, nbig_dev);
+                in, out, sc, oc, a, bp, sc.big, 0, nbig_dev);
             bp.retry = sc.big;
             bp.nretry = nretry + 1;
             orbit_process_big<NWo, CPLX, true><<<ctx->num_sms, 1024, tb, ctx->stream>>>(
-                cur.v, out, sc, ctx->d_oc, a, bp, retry_list, 0, nretry);
+                in, out, sc, oc, a, bp, retry_list, 0, nretry);
             ctx->prof.kernel_launches += 2;
         } else {
             // sc.big -> retry_list (count nretry[1])
             bp.retry = retry_list;
             bp.nretry = nretry + 1;
             orbit_process_big<NWo, CPLX, true><<<ctx->num_sms, 1024, tb, ctx->stream>>>(
-                cur.v, out, sc, ctx->d_oc, a, bp, sc.big, 0, nbig_dev);
+                in, out, sc, oc, a, bp, sc.big, 0, nbig_dev);
             ctx->prof.kernel_launches++;
         }
         OSTEP("orbit_process_big");
@@ -861,7 +865,8 @@ struct Engine {
     // Global-memory passes over the nleft groups left by launch_big_tiers;
     // returns 0 when every group fit, 2 when the output store overflowed, else
     // a negative status.
-    int finish_big_groups(const StoreView& out, OrbitScratch& sc, const OrbitBatchArgs& a, u32 nleft) {
+    int finish_big_groups(const StoreView& in, const StoreView& out, OrbitScratch& sc, const OrbitBatchArgs& a,
+                          u32 nleft, OrbitCounters* oc, OrbitCounters* hoc) {
         constexpr int NWo = PAULI ? NW : 1;
         u32* list = ctx->orbit_team ? sc.big : retry_list;
         u32* other = ctx->orbit_team ? retry_list : sc.big;
@@ -880,21 +885,21 @@ struct Engine {
             CK(cudaMemsetAsync(nretry, 0, 4, ctx->stream));
             {
                 PhaseScope ps(ctx, PH_ROT);
-                orbit_process_big<NWo, CPLX, false><<<grid, 1024, 0, ctx->stream>>>(cur.v, out, sc, ctx->d_oc, a, bp,
-                                                                                   list, nleft, nullptr);
+                orbit_process_big<NWo, CPLX, false><<<grid, 1024, 0, ctx->stream>>>(in, out, sc, oc, a, bp, list,
+                                                                                   nleft, nullptr);
                 OSTEP("orbit_process_big");
                 ctx->prof.kernel_launches++;
             }
             u32 hr = 0;
-            CK(cudaMemcpyAsync(ctx->h_oc, ctx->d_oc, sizeof(OrbitCounters), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(hoc, oc, sizeof(OrbitCounters), cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaMemcpyAsync(&hr, nretry, 4, cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaStreamSynchronize(ctx->stream));
             ctx->prof.syncs++;
-            if (ctx->h_oc->chk_code)
-                return set_err(ctx, FFG_ERR_STATE, "orbit self-check " + std::to_string(ctx->h_oc->chk_code) + " a=" +
-                                                       std::to_string(ctx->h_oc->chk_a) + " b=" + std::to_string(ctx->h_oc->chk_b) +
-                                                       " c=" + std::to_string(ctx->h_oc->chk_c));
-            if (ctx->h_oc->overflow & 1u) return 2;
+            if (hoc->chk_code)
+                return set_err(ctx, FFG_ERR_STATE, "orbit self-check " + std::to_string(hoc->chk_code) + " a=" +
+                                                       std::to_string(hoc->chk_a) + " b=" + std::to_string(hoc->chk_b) +
+                                                       " c=" + std::to_string(hoc->chk_c));
+            if (hoc->overflow & 1u) return 2;
             if (hr == 0) return 0;
             std::swap(list, other);
             nleft = hr;
@@ -945,31 +950,42 @@ struct Engine {
         return sc;
     }
 
-    // Applies rotations [g0, g0+k) of the batch gate table and the batch-end
-    // truncation t (may be null) to the store.  Returns 1 when a group
-    // outgrew the shared-memory table (nothing was changed), else a status.
-    int exec_orbit_batch(int g0, int k, const TruncArgs* t, int maxdeg) {
-        const u64 n_in = ctx->h_ctr->n;  // dense store: no dead entries
-        if (n_in == 0) return FFG_OK;
-        const u64 cap_in = std::max<u64>(n_in, 1024);
-        OrbitScratch sc = carve_scratch(cap_in);
-        if (!sc.amask) return set_err(ctx, FFG_ERR_CUDA, "orbit scratch allocation failed");
+    // One orbit batch: rotations [g0, g0+k) of the batch gate table and the
+    // batch-end truncation t (may be null).
+    struct OrbitJob {
+        int g0, k;
+        const TruncArgs* t;
+    };
+
+    OrbitBatchArgs batch_args(const OrbitJob& j, int maxdeg) const {
         OrbitBatchArgs a{};
-        a.gates = ctx->d_bgates + g0;
-        a.k = k;
+        a.gates = ctx->d_bgates + j.g0;
+        a.k = j.k;
         a.maxdeg = maxdeg;
-        a.thr = t ? t->thr : 0;
-        a.tau = t ? t->tau : 0.0;
-        a.max_xweight = t ? t->max_xweight : -1;
+        a.thr = j.t ? j.t->thr : 0;
+        a.tau = j.t ? j.t->tau : 0.0;
+        a.max_xweight = j.t ? j.t->max_xweight : -1;
         a.route_big = ctx->orbit_route_big;
         if (ctx->batch) {
-            a.inst_cs = ctx->batch->d_inst_cs + (size_t)g0 * ctx->batch->ninst;
+            a.inst_cs = ctx->batch->d_inst_cs + (size_t)j.g0 * ctx->batch->ninst;
             a.ninst = ctx->batch->ninst;
             a.inst_plane = ctx->batch->inst_plane;
             a.inst_shift = ctx->batch->inst_shift;
             a.inst_mask = ctx->batch->inst_mask;
         }
-        u64 out_cap = std::max<u64>(cap, pow2_at_least(4 * n_in));
+        return a;
+    }
+
+    // Runs consecutive orbit batches on the (dense) live store.  Up to
+    // kOrbitWindow batches are enqueued back to back, ping-ponging between the
+    // two store buffers sized for the window, with no host round trip: every
+    // kernel reads its input size from the batch's counters (orbit_gate).  The
+    // host then reads all counters once and walks the batches: completed ones
+    // are committed; at a batch that overflowed (its input is still intact)
+    // the capacity grows and the next window starts there; a batch that left
+    // groups too large for shared memory is finished with global-memory
+    // passes (the batches after it were skipped, so its scratch is intact).
+    int exec_orbit_window(const OrbitJob* jobs, int njobs, int maxdeg) {
         constexpr int NWo = PAULI ? NW : 1;
         const size_t smem = sizeof(OrbitTable<KW, CPLX>) * kOrbitWarps;
         static bool attr_set = false;
@@ -978,85 +994,127 @@ struct Engine {
                                     (int)smem));
             attr_set = true;
         }
-        for (int attempt = 0; attempt < 8; attempt++) {
-            int rc = ensure_buf(ctx, ctx->buf[1 - active], store_bytes(KW, CPLX, out_cap));
+        const int G = ctx->num_sms * 8;
+        int i = 0, regrows = 0;
+        u64 grow = 0;
+        while (i < njobs) {
+            const u64 n_cur = ctx->h_ctr->n;  // dense store: no dead entries
+            if (n_cur == 0) return FFG_OK;  // every later batch is empty too
+            const u64 wcap = std::max<u64>(std::max<u64>(cap, pow2_at_least(4 * n_cur)), grow);
+            int rc = FFG_OK;
+            if (cap < wcap) {
+                rc = compact_into(1 - active, wcap);
+                if (rc) return rc;
+            }
+            rc = ensure_buf(ctx, ctx->buf[1 - active], store_bytes(KW, CPLX, wcap));
             if (rc) return rc;
-            Store dst = carve(ctx->buf[1 - active], KW, CPLX, out_cap);
+            Store S[2] = {cur, carve(ctx->buf[1 - active], KW, CPLX, wcap)};
+            OrbitScratch sc = carve_scratch(wcap);
+            if (!sc.amask) return set_err(ctx, FFG_ERR_CUDA, "orbit scratch allocation failed");
+            const int m = std::min(kOrbitWindow, njobs - i);
             {
                 PhaseScope ps(ctx, PH_ROT);
-                const int g = grid_for(ctx, n_in);
-                orbit_init<<<grid_for(ctx, sc.gmask + 1), kBlock, 0, ctx->stream>>>(ctx->d_oc, sc.gslots,
-                                                                                  sc.gmask + 1, nretry);
-                orbit_classify<NWo, CPLX><<<g, kBlock, 0, ctx->stream>>>(cur.v, n_in, dst.v, sc, ctx->d_oc, a);
-                OSTEP("orbit_classify");
-                orbit_group<KW><<<g, kBlock, 0, ctx->stream>>>(n_in, sc, ctx->d_oc);
-                OSTEP("orbit_group");
-                orbit_offsets<<<1, 1024, 0, ctx->stream>>>(sc, ctx->d_oc);
-                OSTEP("orbit_offsets");
-                orbit_scatter<<<g, kBlock, 0, ctx->stream>>>(n_in, sc);
-                OSTEP("orbit_scatter");
-                orbit_process<NWo, CPLX><<<ctx->num_sms * 2, 32 * kOrbitWarps, smem, ctx->stream>>>(
-                    cur.v, dst.v, sc, ctx->d_oc, a);
-                OSTEP("orbit_process");
-                ctx->prof.kernel_launches += 6;
+                for (int j = 0; j < m; j++) {
+                    const OrbitBatchArgs a = batch_args(jobs[i + j], maxdeg);
+                    OrbitCounters* oc = ctx->d_ocw + j;
+                    const StoreView& in = S[j & 1].v;
+                    const StoreView& out = S[(j + 1) & 1].v;
+                    orbit_gate<<<1, 32, 0, ctx->stream>>>(oc, j ? oc - 1 : nullptr, n_cur, sc.gmask + 1, nretry);
+                    orbit_classify<NWo, CPLX><<<G, kBlock, 0, ctx->stream>>>(in, out, sc, oc, a);
+                    OSTEP("orbit_classify");
+                    orbit_group<KW><<<G, kBlock, 0, ctx->stream>>>(sc, oc);
+                    OSTEP("orbit_group");
+                    orbit_offsets<<<1, 1024, 0, ctx->stream>>>(sc, oc);
+                    OSTEP("orbit_offsets");
+                    orbit_scatter<<<G, kBlock, 0, ctx->stream>>>(sc, oc);
+                    OSTEP("orbit_scatter");
+                    orbit_process<NWo, CPLX><<<ctx->num_sms * 2, 32 * kOrbitWarps, smem, ctx->stream>>>(in, out, sc,
+                                                                                                     oc, a);
+                    OSTEP("orbit_process");
+                    ctx->prof.kernel_launches += 6;
+                    rc = launch_big_tiers(in, out, sc, a, oc);
+                    if (rc) return rc;
+                }
             }
-            int rcb = launch_big_tiers(dst.v, sc, a);
-            if (rcb) return rcb;
             CK(cudaGetLastError());
             u32 nleft = 0;
-            CK(cudaMemcpyAsync(ctx->h_oc, ctx->d_oc, sizeof(OrbitCounters), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(ctx->h_ocw, ctx->d_ocw, m * sizeof(OrbitCounters), cudaMemcpyDeviceToHost,
+                               ctx->stream));
             CK(cudaMemcpyAsync(&nleft, nretry + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaStreamSynchronize(ctx->stream));
             ctx->prof.syncs++;
             if (ctx->profiling) drain_events(ctx);
-            OrbitCounters oc = *ctx->h_oc;
-            if (oc.error) return set_err(ctx, FFG_ERR_STATE, "orbit grouping index overrun");
-            if (oc.chk_code)
-                return set_err(ctx, FFG_ERR_STATE, "orbit self-check " + std::to_string(oc.chk_code) + " a=" +
-                                                       std::to_string(oc.chk_a) + " b=" + std::to_string(oc.chk_b) +
-                                                       " c=" + std::to_string(oc.chk_c));
-            if (oc.overflow & 1u) {
-                out_cap = pow2_at_least(oc.n_out + oc.n_out / 4 + 1024);
-                continue;
-            }
-            if (oc.chk_code == 0 && !(oc.overflow & 1u) && nleft) {
-                const int br = finish_big_groups(dst.v, sc, a, nleft);
-                if (br < 0) return br;
-                oc = *ctx->h_oc;
-                if (br == 2) {
-                    out_cap = pow2_at_least(oc.n_out + oc.n_out / 4 + 1024);
-                    continue;
-                }
-            }
-            ctx->prof.orbit_fallbacks += oc.nbig;  // groups done by the block-level passes
-            ctx->prof.orbit_max_group = std::max<int64_t>(ctx->prof.orbit_max_group, oc.max_members);
-            ctx->prof.orbit_batches++;
-            ctx->prof.orbit_groups += oc.ngroups;
-            if (getenv("FFG_ORBIT_STATS")) {
-                fprintf(stderr, "batch k=%d n_in=%llu groups=%u big=%u wasted=%u out=%llu |", k,
-                        (unsigned long long)n_in, oc.ngroups, oc.nbig, oc.wasted, (unsigned long long)oc.n_out);
-                for (int b = 0; b < 16; b++) fprintf(stderr, " %u", oc.hist[b]);
-                fprintf(stderr, " | A:");
-                for (int b = 0; b < 16; b++) fprintf(stderr, " %u", oc.hist_a[b]);
-                fprintf(stderr, "\n");
-            }
-            // the output store becomes the live store
-            cur = dst;
-            cap = out_cap;
-            active = 1 - active;
-            index_valid = false;
+            int done = 0, live = 0;  // committed batches; S[live] holds the live store
+            bool overflow = false;
             DevCounters h = *ctx->h_ctr;
-            h.apps += (u64)k * n_in + oc.xapps;
-            h.emits += oc.emits;
-            const u64 before_trunc = n_in + oc.created;
-            if (before_trunc > h.peak) h.peak = before_trunc;
-            h.n = oc.n_out;
-            h.alive = oc.n_out;
-            *ctx->h_ctr = h;
-            CK(cudaMemcpyAsync(ctx->d_ctr, ctx->h_ctr, sizeof(DevCounters), cudaMemcpyHostToDevice, ctx->stream));
-            return FFG_OK;
+            for (int j = 0; j < m; j++) {
+                OrbitCounters& oc = ctx->h_ocw[j];
+                if (oc.error) return set_err(ctx, FFG_ERR_STATE, "orbit grouping index overrun");
+                if (oc.chk_code)
+                    return set_err(ctx, FFG_ERR_STATE, "orbit self-check " + std::to_string(oc.chk_code) + " a=" +
+                                                           std::to_string(oc.chk_a) + " b=" + std::to_string(oc.chk_b) +
+                                                           " c=" + std::to_string(oc.chk_c));
+                if (oc.overflow & 1u) {
+                    grow = pow2_at_least(std::max<u64>(oc.n_out + oc.n_out / 4 + 1024, 2 * wcap));
+                    overflow = true;
+                    break;
+                }
+                if (oc.skip) break;
+                const bool last = j == m - 1 || ctx->h_ocw[j + 1].skip;
+                if (last && nleft) {
+                    const OrbitBatchArgs a = batch_args(jobs[i + j], maxdeg);
+                    const int br = finish_big_groups(S[j & 1].v, S[(j + 1) & 1].v, sc, a, nleft, ctx->d_ocw + j, &oc);
+                    if (br < 0) return br;
+                    if (br == 2) {
+                        grow = pow2_at_least(std::max<u64>(oc.n_out + oc.n_out / 4 + 1024, 2 * wcap));
+                        overflow = true;
+                        break;
+                    }
+                }
+                // commit batch j
+                const OrbitJob& jb = jobs[i + j];
+                ctx->prof.orbit_fallbacks += oc.nbig;  // groups done by the block-level passes
+                ctx->prof.orbit_max_group = std::max<int64_t>(ctx->prof.orbit_max_group, oc.max_members);
+                ctx->prof.orbit_batches++;
+                ctx->prof.orbit_groups += oc.ngroups;
+                if (getenv("FFG_ORBIT_STATS")) {
+                    fprintf(stderr, "batch k=%d n_in=%llu groups=%u big=%u wasted=%u out=%llu |", jb.k,
+                            (unsigned long long)oc.n_in, oc.ngroups, oc.nbig, oc.wasted,
+                            (unsigned long long)oc.n_out);
+                    for (int b = 0; b < 16; b++) fprintf(stderr, " %u", oc.hist[b]);
+                    fprintf(stderr, " | A:");
+                    for (int b = 0; b < 16; b++) fprintf(stderr, " %u", oc.hist_a[b]);
+                    fprintf(stderr, "\n");
+                }
+                h.apps += (u64)jb.k * oc.n_in + oc.xapps;
+                h.emits += oc.emits;
+                const u64 before_trunc = oc.n_in + oc.created;
+                if (before_trunc > h.peak) h.peak = before_trunc;
+                h.n = oc.n_out;
+                h.alive = oc.n_out;
+                live = (j + 1) & 1;
+                done++;
+                if (h.n == 0) break;
+            }
+            if (done) {
+                cur = S[live];
+                if (live == 1) active = 1 - active;
+                cap = wcap;
+                index_valid = false;
+                *ctx->h_ctr = h;
+                CK(cudaMemcpyAsync(ctx->d_ctr, ctx->h_ctr, sizeof(DevCounters), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+                i += done;
+                if (h.n == 0) return FFG_OK;
+            } else {
+                cap = wcap;  // the live store stays in place (S[0])
+            }
+            if (overflow) {
+                ctx->prof.regrows++;
+                if (++regrows > 64) return set_err(ctx, FFG_ERR_STATE, "orbit batch: output store kept overflowing");
+            }
         }
-        return set_err(ctx, FFG_ERR_STATE, "orbit batch: output store kept overflowing");
+        return FFG_OK;
     }
 
     // Batch gate table (one entry per GROUP op, in op order); gate_of_op maps an
@@ -1178,9 +1236,8 @@ struct Engine {
             if (!rc) rc = sync_counters();
             return rc;
         }
-        int rc = exec_orbit_batch(r.g0, r.k, r.has_trunc ? &r.trunc : nullptr, maxdeg);
-        if (rc == 1) return set_err(ctx, FFG_ERR_STATE, "batched propagation: orbit group larger than 2^26 terms");
-        return rc;
+        const OrbitJob job{r.g0, r.k, r.has_trunc ? &r.trunc : nullptr};
+        return exec_orbit_window(&job, 1, maxdeg);
     }
 
     // Pauli batched runs: long commuting runs go through the batch-orbit path,
@@ -1194,41 +1251,43 @@ struct Engine {
         rc = upload_batch_gates(ops, groups, gate_of_op);
         if (rc) return rc;
         size_t pos = 0;  // next op to execute
+        std::vector<OrbitJob> jobs;  // consecutive orbit batches not yet run
+        auto flush = [&]() -> int {
+            if (jobs.empty()) return FFG_OK;
+            const int r = exec_orbit_window(jobs.data(), (int)jobs.size(), maxdeg);
+            jobs.clear();
+            return r;
+        };
         for (const BatchInfo& b : batches) {
             if (b.nrot < ctx->orbit_min_gates) continue;
             const int end = b.trunc >= 0 ? b.trunc + 1 : b.first + b.nrot;
             if (b.trunc >= 0 && ops[b.trunc].topk > 0) continue;
             // ops before this batch go through the persistent kernel
             if (pos < (size_t)b.first) {
+                rc = flush();
+                if (rc) return rc;
                 rc = exec_persistent(pos, b.first);
                 if (rc) return rc;
+                // the orbit path reads a dense store (the host counters are
+                // current after a persistent run)
+                if (ctx->h_ctr->n != ctx->h_ctr->alive) {
+                    rc = compact_into(1 - active, cap);
+                    if (rc) return rc;
+                    rc = sync_counters();
+                    if (rc) return rc;
+                }
             }
-            // the host counters are current here: the persistent run and the
-            // orbit batch both leave them up to date
-            if (ctx->h_ctr->n != ctx->h_ctr->alive) {
-                rc = compact_into(1 - active, cap);  // the orbit path reads a dense store
-                if (rc) return rc;
-                rc = sync_counters();
-                if (rc) return rc;
-            }
-            // split runs longer than the batch gate limit
-            int done = 0, st = FFG_OK;
-            while (done < b.nrot && st == FFG_OK) {
+            // runs longer than the batch gate limit are split
+            for (int done = 0; done < b.nrot;) {
                 const int k = std::min(kMaxBatchGates, b.nrot - done);
                 const bool last = done + k == b.nrot;
-                const TruncArgs* t = (last && b.trunc >= 0) ? &truncs[ops[b.trunc].idx] : nullptr;
-                st = exec_orbit_batch(gate_of_op[b.first + done], k, t, maxdeg);
-                if (st == 1) break;
-                if (st) return st;
+                jobs.push_back({gate_of_op[b.first + done], k, (last && b.trunc >= 0) ? &truncs[ops[b.trunc].idx] : nullptr});
                 done += k;
-            }
-            if (st == 1) {
-                // a group too large for shared memory: finish this batch per gate
-                rc = exec_persistent(b.first + done, end);
-                if (rc) return rc;
             }
             pos = end;
         }
+        rc = flush();
+        if (rc) return rc;
         if (pos < ops.size()) {
             rc = exec_persistent(pos, ops.size());
             if (rc) return rc;
@@ -1724,13 +1783,12 @@ int batch_adjoint(ffg_batch* h, const double* weights, double* grad_theta, doubl
             A.abar_in = B.abar_in;
             A.grad = B.grad + (size_t)rec.g0 * ninst;
             A.err = B.err;
-            CK(cudaMemsetAsync(ctx->d_oc, 0, sizeof(OrbitCounters), ctx->stream));
-            CK(cudaMemsetAsync(sc.gslots, 0xff, (sc.gmask + 1) * 8, ctx->stream));
             const int g = grid_for(ctx, n_in);
-            orbit_classify<NW, false><<<g, kBlock, 0, ctx->stream>>>(in, n_in, dummy.v, sc, ctx->d_oc, a);
-            orbit_group<KW><<<g, kBlock, 0, ctx->stream>>>(n_in, sc, ctx->d_oc);
+            orbit_gate<<<1, 32, 0, ctx->stream>>>(ctx->d_oc, nullptr, n_in, sc.gmask + 1, E.nretry);
+            orbit_classify<NW, false><<<g, kBlock, 0, ctx->stream>>>(in, dummy.v, sc, ctx->d_oc, a);
+            orbit_group<KW><<<g, kBlock, 0, ctx->stream>>>(sc, ctx->d_oc);
             orbit_offsets<<<1, 1024, 0, ctx->stream>>>(sc, ctx->d_oc);
-            orbit_scatter<<<g, kBlock, 0, ctx->stream>>>(n_in, sc);
+            orbit_scatter<<<g, kBlock, 0, ctx->stream>>>(sc, ctx->d_oc);
             adj_passthrough<KW><<<g, kBlock, 0, ctx->stream>>>(in, n_in, sc, A);
             adj_orbit_warp<NW><<<ctx->num_sms * 2, 32 * kAdjWarps, warp_smem, ctx->stream>>>(in, sc, ctx->d_oc, A);
             CK(cudaGetLastError());
@@ -1830,6 +1888,8 @@ int ffg_create(ffg_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ps, sizeof(PersistState));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_oc, sizeof(OrbitCounters));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_oc, sizeof(OrbitCounters));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ocw, kOrbitWindow * sizeof(OrbitCounters));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_ocw, kOrbitWindow * sizeof(OrbitCounters));
     if (e != cudaSuccess) {
         fprintf(stderr, "ffg_create: %s\n", cudaGetErrorString(e));
         ffg_destroy(ctx);
@@ -1860,6 +1920,8 @@ int ffg_destroy(ffg_ctx* ctx) {
     if (ctx->bigpool.p) cudaFree(ctx->bigpool.p);
     if (ctx->d_oc) cudaFree(ctx->d_oc);
     if (ctx->h_oc) cudaFreeHost(ctx->h_oc);
+    if (ctx->d_ocw) cudaFree(ctx->d_ocw);
+    if (ctx->h_ocw) cudaFreeHost(ctx->h_ocw);
     if (ctx->d_ctr) cudaFree(ctx->d_ctr);
     if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
     for (auto e : ctx->free_events) cudaEventDestroy(e);

@@ -73,6 +73,9 @@ struct OrbitCounters {
     u32 hist[16];      // completed groups by floor(log2(final members))
     u32 hist_a[16];    // completed groups by |A| (capped at 15)
     u32 wasted;        // groups abandoned by the warp pass after growing past its table
+    u32 skip;          // 1: an earlier batch of the window did not complete; this one does nothing
+    u64 n_in;          // terms entering the batch (set by orbit_gate)
+    u64 gmask;         // group-index slots - 1 for this batch (set by orbit_gate)
 };
 
 #ifdef FFG_ORBIT_CHECK
@@ -156,27 +159,54 @@ __device__ __forceinline__ void out_append(const StoreView& o, OrbitCounters* oc
     o.dead[pos] = 0;
 }
 
-// Per-batch reset: counters, the group index and the two retry counts.
-__global__ void __launch_bounds__(kBlock) orbit_init(OrbitCounters* oc, u64* gslots, u64 nslots, u32* nretry) {
-    const u64 stride = (u64)gridDim.x * blockDim.x;
-    const u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x;
-    for (u64 i = t; i < nslots; i += stride) gslots[i] = ~0ull;
+// Opens a batch (one warp): clears its counters and, unless an earlier batch
+// of the window did not complete (overflowed its output store, failed a
+// check, or left groups for the host in nretry[1]), sets the number of input
+// terms (the previous batch's output, or n_first) and the group-index size,
+// and clears the two retry counts.  Otherwise the batch is marked skipped and
+// every kernel of it returns at once, leaving the scratch as the incomplete
+// batch left it.
+__global__ void orbit_gate(OrbitCounters* cur, const OrbitCounters* prev, u64 n_first, u64 gslots_cap,
+                           u32* nretry) {
     constexpr u32 nw = sizeof(OrbitCounters) / 4;
-    for (u64 i = t; i < nw; i += stride) ((u32*)oc)[i] = 0;
-    if (t < 2) nretry[t] = 0;
+    for (u32 i = threadIdx.x; i < nw; i += blockDim.x) ((u32*)cur)[i] = 0;
+    __syncwarp();
+    if (threadIdx.x != 0) return;
+    const bool bad = prev && (prev->skip || (prev->overflow & 1u) || prev->error || prev->chk_code ||
+                              nretry[1] != 0);
+    if (bad) {
+        cur->skip = 1;
+        return;
+    }
+    const u64 n = prev ? prev->n_out : n_first;
+    u64 slots = 1024;
+    while (slots < 2 * n) slots <<= 1;
+    if (slots > gslots_cap) {  // more input terms than the window was sized for
+        cur->skip = 1;
+        cur->overflow = 1;
+        cur->n_out = n;
+        return;
+    }
+    cur->n_in = n;
+    cur->gmask = slots - 1;
+    nretry[0] = 0;
+    nretry[1] = 0;
 }
 
 // A(Q) for every input term; group key; final terms go to the output.
 template <int NW, bool CPLX>
-__global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, u64 n_in, StoreView out,
-                                                         OrbitScratch sc, OrbitCounters* oc,
-                                                         OrbitBatchArgs a) {
+__global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, StoreView out, OrbitScratch sc,
+                                                         OrbitCounters* oc, OrbitBatchArgs a) {
     constexpr int KW = 2 * NW;
+    if (*(volatile u32*)&oc->skip) return;
+    const u64 n_in = *(volatile u64*)&oc->n_in;
+    const u64 nslots = *(volatile u64*)&oc->gmask + 1;
     __shared__ u64 gp[kMaxBatchGates][KW];
     for (int t = threadIdx.x; t < a.k; t += blockDim.x)
         for (int w = 0; w < KW; w++) gp[t][w] = a.gates[t].p[w];
     __syncthreads();
     const u64 stride = (u64)gridDim.x * blockDim.x;
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += stride) sc.gslots[i] = kEmptySlot;
     for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += stride) {
         u64 q[KW];
         load_key<KW>(in, i, q);
@@ -234,15 +264,18 @@ __device__ __forceinline__ bool same_group(const OrbitScratch& sc, u64 i, u64 j)
 
 // representative of each term's group: the term that claims the index slot
 template <int KW>
-__global__ void __launch_bounds__(kBlock) orbit_group(u64 n_in, OrbitScratch sc, OrbitCounters* oc) {
+__global__ void __launch_bounds__(kBlock) orbit_group(OrbitScratch sc, OrbitCounters* oc) {
+    if (*(volatile u32*)&oc->skip) return;
+    const u64 n_in = *(volatile u64*)&oc->n_in;
+    const u64 gmask = *(volatile u64*)&oc->gmask;
     const u64 stride = (u64)gridDim.x * blockDim.x;
     for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += stride) {
         if (sc.rep[i] == 0xffffffffu) continue;
         const u64 h = group_hash<KW>(sc, i);
         const u32 fp = (u32)(h >> 32);
-        u64 pos = h & sc.gmask;
+        u64 pos = h & gmask;
         u32 rep = 0xffffffffu;
-        for (u64 probe = 0; probe <= sc.gmask; probe++) {
+        for (u64 probe = 0; probe <= gmask; probe++) {
             u64 e = __ldcg(&sc.gslots[pos]);
             if (e == kEmptySlot) {
                 e = atomicCAS(&sc.gslots[pos], kEmptySlot, ((u64)fp << 32) | i);
@@ -255,7 +288,7 @@ __global__ void __launch_bounds__(kBlock) orbit_group(u64 n_in, OrbitScratch sc,
                 rep = (u32)e;
                 break;
             }
-            pos = (pos + 1) & sc.gmask;
+            pos = (pos + 1) & gmask;
         }
         if (rep == 0xffffffffu) {
             atomicOr(&oc->error, 1u);
@@ -305,7 +338,9 @@ __global__ void __launch_bounds__(1024) orbit_offsets(OrbitScratch sc, OrbitCoun
     }
 }
 
-__global__ void __launch_bounds__(kBlock) orbit_scatter(u64 n_in, OrbitScratch sc) {
+__global__ void __launch_bounds__(kBlock) orbit_scatter(OrbitScratch sc, const OrbitCounters* oc) {
+    if (*(volatile const u32*)&oc->skip) return;
+    const u64 n_in = *(volatile const u64*)&oc->n_in;
     const u64 stride = (u64)gridDim.x * blockDim.x;
     for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += stride) {
         const u32 r = sc.rep[i];
@@ -624,6 +659,7 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
     constexpr int KW = 2 * NW;
     __shared__ long long red[3][32];
     extern __shared__ __align__(16) unsigned char btab[];
+    if (*(volatile u32*)&oc->skip) return;
     if (nlist_dev) nlist = *(volatile const u32*)nlist_dev;  // list length written by an earlier kernel
     long long emits = 0, created = 0, xapps = 0;
     for (u32 gi = blockIdx.x; gi < nlist; gi += gridDim.x) {
