@@ -108,14 +108,6 @@ __device__ __forceinline__ void adj_insert(const AdjTable<KW>& T, const u64* k, 
     }
 }
 
-template <int TEAM>
-__device__ __forceinline__ void team_sync() {
-    if (TEAM == 32)
-        __syncwarp();
-    else
-        __syncthreads();
-}
-
 struct AdjArgs {
     OrbitBatchArgs a;     // the batch (gates, k, maxdeg, truncation, instances)
     StoreView out;        // term set after the batch (index over its live keys)

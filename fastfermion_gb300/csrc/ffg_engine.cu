@@ -33,6 +33,7 @@
 #include "ffg_persist.cuh"
 #include "ffg_orbit.cuh"
 #include "ffg_adjoint.cuh"
+#include "ffg_morbit.cuh"
 
 using namespace ffg;
 
@@ -173,6 +174,10 @@ struct ffg_ctx {
     int orbit_min_gates = 4;    // shortest run sent to the batch-orbit path
     int orbit_route_big = 8;    // |A| from which a group skips the warp-level pass (FFG_ORBIT_ROUTE)
     bool orbit_team = true;     // 256-thread team pass before the 1024-thread pass (FFG_ORBIT_TEAM=0 disables)
+    bool morbit = true;         // batch-orbit path for commuting Majorana runs (FFG_MORBIT=0 disables)
+    int morbit_min_gates = 2;   // shortest Majorana run sent to the batch-orbit path
+    MBatchGate* d_mgates = nullptr;
+    size_t mgates_cap = 0;
     BatchGate* d_bgates = nullptr;
     size_t bgates_cap = 0;
     char* d_oscratch = nullptr;
@@ -1024,7 +1029,7 @@ struct Engine {
                     OSTEP("orbit_classify");
                     orbit_group<KW><<<G, kBlock, 0, ctx->stream>>>(sc, oc);
                     OSTEP("orbit_group");
-                    orbit_offsets<<<1, 1024, 0, ctx->stream>>>(sc, oc);
+                    orbit_offsets<<<G, kBlock, 0, ctx->stream>>>(sc, oc);
                     OSTEP("orbit_offsets");
                     orbit_scatter<<<G, kBlock, 0, ctx->stream>>>(sc, oc);
                     OSTEP("orbit_scatter");
@@ -1115,6 +1120,192 @@ struct Engine {
             }
         }
         return FFG_OK;
+    }
+
+    // ---------------------------------------------------------------------
+    // Majorana runs (batch-orbit path with the threshold after every gate)
+    // ---------------------------------------------------------------------
+    int upload_mgates(const std::vector<RotArgs>& rots) {
+        std::vector<MBatchGate> mg(rots.size());
+        for (size_t i = 0; i < rots.size(); i++) {
+            MBatchGate g{};
+            for (int w = 0; w < 4; w++) {
+                g.p[w] = rots[i].p[w];
+                g.mg[w] = rots[i].mg[w];
+            }
+            g.c = rots[i].c;
+            g.fr = rots[i].fr;
+            g.fi = rots[i].fi;
+            g.odd = rots[i].gate_odd;
+            mg[i] = g;
+        }
+        return upload(ctx->d_mgates, ctx->mgates_cap, mg);
+    }
+
+    // Gates [g0, g0 + k) of the Majorana gate table (application order), all
+    // mutually commuting, each followed by the threshold of t, on the dense
+    // live store.
+    int exec_morbit_batch(int g0, int k, const TruncArgs& t, int maxdeg) {
+        const u64 n_in = ctx->h_ctr->n;
+        if (n_in == 0) return FFG_OK;
+        const u64 cap_in = std::max<u64>(n_in, 1024);
+        OrbitScratch sc = carve_scratch(cap_in);
+        if (!sc.amask) return set_err(ctx, FFG_ERR_CUDA, "orbit scratch allocation failed");
+        MOrbitArgs a{};
+        a.gates = ctx->d_mgates + g0;
+        a.k = k;
+        a.maxdeg = maxdeg;
+        a.thr = t.thr;
+        a.tau = t.tau;
+        a.route_big = ctx->orbit_route_big;
+        const size_t wsm = (size_t)kMWarps * mtable_bytes<KW>(kMWarpCap);
+        const size_t tsm = mtable_bytes<KW>(kMTeamCap);
+        static bool attr_set = false;
+        static int team_per_sm = 1;
+        if (!attr_set) {
+            CK(cudaFuncSetAttribute(morbit_warp<KW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+            CK(cudaFuncSetAttribute(morbit_block<KW, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)tsm));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&team_per_sm, morbit_block<KW, 256, true>, 256, tsm));
+            team_per_sm = std::max(team_per_sm, 1);
+            attr_set = true;
+        }
+        u64 out_cap = std::max<u64>(cap, pow2_at_least(4 * n_in));
+        const int G = ctx->num_sms * 8;
+        for (int attempt = 0; attempt < 8; attempt++) {
+            int rc = ensure_buf(ctx, ctx->buf[1 - active], store_bytes(KW, true, out_cap));
+            if (rc) return rc;
+            Store dst = carve(ctx->buf[1 - active], KW, true, out_cap);
+            OrbitCounters* oc = ctx->d_oc;
+            {
+                PhaseScope ps(ctx, PH_ROT);
+                orbit_gate<<<1, 32, 0, ctx->stream>>>(oc, nullptr, n_in, sc.gmask + 1, nretry);
+                morbit_classify<KW><<<G, kBlock, 0, ctx->stream>>>(cur.v, dst.v, sc, oc, a);
+                OSTEP("morbit_classify");
+                orbit_group<KW><<<G, kBlock, 0, ctx->stream>>>(sc, oc);
+                orbit_offsets<<<G, kBlock, 0, ctx->stream>>>(sc, oc);
+                orbit_scatter<<<G, kBlock, 0, ctx->stream>>>(sc, oc);
+                OSTEP("orbit_scatter");
+                morbit_single<KW><<<G, kBlock, 0, ctx->stream>>>(cur.v, dst.v, sc, oc, a);
+                OSTEP("morbit_single");
+                morbit_warp<KW><<<ctx->num_sms * 2, 32 * kMWarps, wsm, ctx->stream>>>(cur.v, dst.v, sc, oc, a);
+                OSTEP("morbit_warp");
+                morbit_block<KW, 256, true><<<ctx->num_sms * team_per_sm, 256, tsm, ctx->stream>>>(
+                    cur.v, dst.v, sc, oc, a, kMTeamCap, nullptr, 0, sc.big, 0, &oc->nbig, retry_list, nretry);
+                OSTEP("morbit_block");
+                ctx->prof.kernel_launches += 8;
+            }
+            u32 nleft = 0;
+            CK(cudaMemcpyAsync(ctx->h_oc, oc, sizeof(OrbitCounters), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(&nleft, nretry, 4, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            ctx->prof.syncs++;
+            if (ctx->profiling) drain_events(ctx);
+            if (ctx->h_oc->error) return set_err(ctx, FFG_ERR_STATE, "orbit grouping index overrun");
+            bool overflow = (ctx->h_oc->overflow & 1u) != 0;
+            u32* list = retry_list;
+            u32* other = sc.big;
+            u32 rcap = 4096;
+            while (!overflow && nleft > 0) {
+                if (rcap > (1u << 22)) return set_err(ctx, FFG_ERR_STATE, "Majorana orbit group larger than 2^22 terms");
+                const u32 grid = std::min<u32>(nleft, (u32)ctx->num_sms);
+                const u64 region = mtable_bytes<KW>(rcap);
+                rc = ensure_buf(ctx, ctx->bigpool, region * grid);
+                if (rc) return rc;
+                CK(cudaMemsetAsync(nretry + 1, 0, 4, ctx->stream));
+                {
+                    PhaseScope ps(ctx, PH_ROT);
+                    morbit_block<KW, 1024, false><<<grid, 1024, 0, ctx->stream>>>(
+                        cur.v, dst.v, sc, oc, a, rcap, ctx->bigpool.p, region, list, nleft, nullptr, other, nretry + 1);
+                    OSTEP("morbit_block");
+                    ctx->prof.kernel_launches++;
+                }
+                u32 hr = 0;
+                CK(cudaMemcpyAsync(ctx->h_oc, oc, sizeof(OrbitCounters), cudaMemcpyDeviceToHost, ctx->stream));
+                CK(cudaMemcpyAsync(&hr, nretry + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
+                CK(cudaStreamSynchronize(ctx->stream));
+                ctx->prof.syncs++;
+                overflow = (ctx->h_oc->overflow & 1u) != 0;
+                std::swap(list, other);
+                nleft = hr;
+                rcap *= 4;
+            }
+            const OrbitCounters oc_h = *ctx->h_oc;
+            if (overflow) {
+                out_cap = pow2_at_least(oc_h.n_out + oc_h.n_out / 4 + 1024);
+                ctx->prof.regrows++;
+                continue;
+            }
+            ctx->prof.orbit_batches++;
+            ctx->prof.orbit_groups += oc_h.ngroups;
+            ctx->prof.orbit_fallbacks += oc_h.nbig;
+            cur = dst;
+            cap = out_cap;
+            active = 1 - active;
+            index_valid = false;
+            DevCounters h = *ctx->h_ctr;
+            h.apps += oc_h.xapps;
+            h.emits += oc_h.emits;
+            if (oc_h.n_out > h.peak) h.peak = oc_h.n_out;
+            h.n = oc_h.n_out;
+            h.alive = oc_h.n_out;
+            *ctx->h_ctr = h;
+            CK(cudaMemcpyAsync(ctx->d_ctr, ctx->h_ctr, sizeof(DevCounters), cudaMemcpyHostToDevice, ctx->stream));
+            return FFG_OK;
+        }
+        return set_err(ctx, FFG_ERR_STATE, "Majorana orbit batch: output store kept overflowing");
+    }
+
+    // Majorana circuit: commuting runs (gate ranges, application order) of at
+    // least morbit_min_gates gates go through the orbit path, the rest (and
+    // the first gate, so that every run starts from thresholded terms)
+    // through the persistent per-gate kernel.
+    int run_majorana(const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
+                     const std::vector<TruncArgs>& truncs, const std::vector<std::pair<int, int>>& runs,
+                     int maxdeg) {
+        int rc = prepare_persistent(ops, rots, truncs, {});
+        if (rc) return rc;
+        rc = upload_mgates(rots);
+        if (rc) return rc;
+        const bool thr = !truncs.empty() && truncs[0].thr;
+        const size_t opg = thr ? 2 : 1;  // ops per gate: the rotation, then the threshold
+        const TruncArgs t = thr ? truncs[0] : TruncArgs{};
+        size_t p0 = 0, p1 = 0;           // pending persistent ops [p0, p1)
+        auto flush = [&]() -> int {
+            int r = FFG_OK;
+            if (p1 > p0) r = exec_persistent(p0, p1);
+            p0 = p1;
+            return r;
+        };
+        for (const auto& run : runs) {
+            int g = run.first;
+            const int g1 = run.second;
+            if (g == 0) g = 1;  // the first gate runs per gate (it also thresholds the input)
+            if (g1 - g < ctx->morbit_min_gates) {
+                p1 = (size_t)g1 * opg;
+                continue;
+            }
+            p1 = (size_t)g * opg;
+            rc = flush();
+            if (rc) return rc;
+            if (ctx->h_ctr->n != ctx->h_ctr->alive) {
+                rc = compact_into(1 - active, cap);
+                if (rc) return rc;
+                rc = sync_counters();
+                if (rc) return rc;
+            }
+            for (int done = g; done < g1;) {
+                const int k = std::min(kMaxBatchGates, g1 - done);
+                rc = exec_morbit_batch(done, k, t, maxdeg);
+                if (rc) return rc;
+                done += k;
+            }
+            p0 = p1 = (size_t)g1 * opg;
+        }
+        p1 = ops.size();
+        rc = flush();
+        if (rc) return rc;
+        return finish();
     }
 
     // Batch gate table (one entry per GROUP op, in op order); gate_of_op maps an
@@ -1530,13 +1721,15 @@ int run_engine(ffg_ctx* ctx, const uint64_t* keys, const double* re, const doubl
                int on_device, const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
                const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups,
                bool deterministic, ffg_result** out, const std::vector<BatchInfo>* binfo = nullptr,
-               int maxdeg = 128) {
+               int maxdeg = 128, const std::vector<std::pair<int, int>>* mruns = nullptr) {
     Engine<KW, CPLX, PAULI> E(ctx);
     int rc = E.load(keys, re, im, n, on_device, 0);
     if (rc) return rc;
     bool has_topk = false;
     for (const Op& o : ops) has_topk = has_topk || (o.type == Op::TRUNC && o.topk > 0);
-    if (has_topk)
+    if (!PAULI && mruns && ctx->morbit && ctx->persistent)
+        rc = E.run_majorana(ops, rots, truncs, *mruns, maxdeg);
+    else if (has_topk)
         rc = E.run(ops, rots, truncs, groups);
     else if (PAULI && binfo && ctx->orbit && ctx->persistent && ctx->group_d == 1)
         rc = E.run_mixed(ops, rots, truncs, groups, *binfo, maxdeg);
@@ -1787,7 +1980,7 @@ int batch_adjoint(ffg_batch* h, const double* weights, double* grad_theta, doubl
             orbit_gate<<<1, 32, 0, ctx->stream>>>(ctx->d_oc, nullptr, n_in, sc.gmask + 1, E.nretry);
             orbit_classify<NW, false><<<g, kBlock, 0, ctx->stream>>>(in, dummy.v, sc, ctx->d_oc, a);
             orbit_group<KW><<<g, kBlock, 0, ctx->stream>>>(sc, ctx->d_oc);
-            orbit_offsets<<<1, 1024, 0, ctx->stream>>>(sc, ctx->d_oc);
+            orbit_offsets<<<g, kBlock, 0, ctx->stream>>>(sc, ctx->d_oc);
             orbit_scatter<<<g, kBlock, 0, ctx->stream>>>(sc, ctx->d_oc);
             adj_passthrough<KW><<<g, kBlock, 0, ctx->stream>>>(in, n_in, sc, A);
             adj_orbit_warp<NW><<<ctx->num_sms * 2, 32 * kAdjWarps, warp_smem, ctx->stream>>>(in, sc, ctx->d_oc, A);
@@ -1878,6 +2071,8 @@ int ffg_create(ffg_ctx** out, int device) {
     if (const char* d = getenv("FFG_ORBIT_MIN")) ctx->orbit_min_gates = std::max(1, atoi(d));
     if (const char* d = getenv("FFG_ORBIT_ROUTE")) ctx->orbit_route_big = std::max(1, atoi(d));
     if (const char* d = getenv("FFG_ORBIT_TEAM")) ctx->orbit_team = atoi(d) != 0;
+    if (const char* d = getenv("FFG_MORBIT")) ctx->morbit = atoi(d) != 0;
+    if (const char* d = getenv("FFG_MORBIT_MIN")) ctx->morbit_min_gates = std::max(1, atoi(d));
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -1916,6 +2111,7 @@ int ffg_destroy(ffg_ctx* ctx) {
     if (ctx->d_truncs) cudaFree(ctx->d_truncs);
     if (ctx->d_groups2) cudaFree(ctx->d_groups2);
     if (ctx->d_bgates) cudaFree(ctx->d_bgates);
+    if (ctx->d_mgates) cudaFree(ctx->d_mgates);
     if (ctx->d_oscratch) cudaFree(ctx->d_oscratch);
     if (ctx->bigpool.p) cudaFree(ctx->bigpool.p);
     if (ctx->d_oc) cudaFree(ctx->d_oc);
@@ -2082,13 +2278,38 @@ int ffg_majorana_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re,
             if (t.thr) ops.push_back({Op::TRUNC, 0, 0, 0, 0});
         }
         ctx->prof.n_gates = (int64_t)rots.size();
+        // maximal runs of mutually commuting gates, application order
+        // (commutation of Majorana strings: |a||b| - |a & b| even,
+        // src/majorana_algebra.h:79-84)
+        std::vector<std::pair<int, int>> runs;
+        {
+            auto commute = [&](const RotArgs& x, const RotArgs& y) {
+                int dx = 0, dy = 0, dxy = 0;
+                for (int w = 0; w < 4; w++) {
+                    dx += popc64(x.p[w]);
+                    dy += popc64(y.p[w]);
+                    dxy += popc64(x.p[w] & y.p[w]);
+                }
+                return ((dx * dy - dxy) & 1) == 0;
+            };
+            int s0 = 0;
+            for (int g = 1; g <= (int)rots.size(); g++) {
+                bool ok = g < (int)rots.size();
+                for (int u = s0; u < g && ok; u++) ok = commute(rots[u], rots[g]);
+                if (!ok) {
+                    runs.push_back({s0, g});
+                    s0 = g;
+                }
+            }
+        }
         const bool det = params->deterministic != 0;
+        const int md = params->has_maxdegree ? params->maxdegree : 1 << 30;
         int rc;
         switch (kw) {
-            case 1: rc = run_engine<1, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out); break;
-            case 2: rc = run_engine<2, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out); break;
-            case 3: rc = run_engine<3, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out); break;
-            default: rc = run_engine<4, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out); break;
+            case 1: rc = run_engine<1, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out, nullptr, md, &runs); break;
+            case 2: rc = run_engine<2, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out, nullptr, md, &runs); break;
+            case 3: rc = run_engine<3, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out, nullptr, md, &runs); break;
+            default: rc = run_engine<4, true, false>(ctx, keys, re, im, n, on_device, ops, rots, truncs, {}, det, out, nullptr, md, &runs); break;
         }
         ctx->prof.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return rc;

@@ -74,6 +74,8 @@ struct OrbitCounters {
     u32 hist_a[16];    // completed groups by |A| (capped at 15)
     u32 wasted;        // groups abandoned by the warp pass after growing past its table
     u32 skip;          // 1: an earlier batch of the window did not complete; this one does nothing
+    u32 member_total;  // members placed by orbit_offsets
+    u32 nrest;         // groups left by a thread-level pass for the warp tier (list in OrbitScratch::fill)
     u64 n_in;          // terms entering the batch (set by orbit_gate)
     u64 gmask;         // group-index slots - 1 for this batch (set by orbit_gate)
 };
@@ -110,6 +112,15 @@ struct OrbitBatchArgs {
     int inst_shift;
     u64 inst_mask;
 };
+
+// barrier of a team of TEAM threads (a warp, or the whole block)
+template <int TEAM>
+__device__ __forceinline__ void team_sync() {
+    if (TEAM == 32)
+        __syncwarp();
+    else
+        __syncthreads();
+}
 
 // instance of the group represented by input position rep
 __device__ __forceinline__ u32 group_instance(const StoreView& in, const OrbitBatchArgs& a, u32 rep) {
@@ -303,38 +314,30 @@ __global__ void __launch_bounds__(kBlock) orbit_group(OrbitScratch sc, OrbitCoun
     }
 }
 
-// first member position of every group (groups listed in sc.groups)
-__global__ void __launch_bounds__(1024) orbit_offsets(OrbitScratch sc, OrbitCounters* oc) {
+// first member position of every group (groups listed in sc.groups).  Any
+// placement of the groups works (each group is processed on its own), so the
+// ranges come from warp-aggregated atomic additions, in parallel.
+__global__ void __launch_bounds__(kBlock) orbit_offsets(OrbitScratch sc, OrbitCounters* oc) {
+    if (*(volatile u32*)&oc->skip) return;
     const u32 ng = *(volatile u32*)&oc->ngroups;
-    __shared__ u32 carry;
-    __shared__ u32 wt[32];
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (u32 base = 0; base < ng; base += blockDim.x) {
-        const u32 g = base + threadIdx.x;
-        const u32 v = g < ng ? sc.cnt[sc.groups[g]] : 0u;
+    const int lane = threadIdx.x & 31;
+    const u32 stride = gridDim.x * blockDim.x;
+    // every warp runs the same number of iterations so that the shuffles see full warps
+    const u32 tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const u32 rounds = (ng + stride - 1) / stride;
+    for (u32 r = 0; r < rounds; r++) {
+        const u32 g = tid + r * stride;
+        const u32 rep = g < ng ? sc.groups[g] : 0u;
+        const u32 v = g < ng ? sc.cnt[rep] : 0u;
         u32 x = v;
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         for (int o = 1; o < 32; o <<= 1) {
             const u32 y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
         }
-        if (lane == 31) wt[wid] = x;
-        __syncthreads();
-        if (wid == 0) {
-            u32 w = lane < (int)(blockDim.x >> 5) ? wt[lane] : 0u;
-            for (int o = 1; o < 32; o <<= 1) {
-                const u32 y = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= o) w += y;
-            }
-            wt[lane] = w;
-        }
-        __syncthreads();
-        const u32 incl = x + (wid > 0 ? wt[wid - 1] : 0u);
-        if (g < ng) sc.off[sc.groups[g]] = carry + incl - v;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry += incl;
-        __syncthreads();
+        u32 base = 0;
+        if (lane == 31 && x) base = atomicAdd(&oc->member_total, x);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        if (g < ng) sc.off[rep] = base + x - v;
     }
 }
 

@@ -72,7 +72,8 @@ def test_deterministic_mode_repeats():
 
 def test_apps_counter_matches_oracle():
     from fastfermion_gb300 import _native
-    for name in ("cfg1_chain", "cfg1_chain_unbatched", "ref_mixed_clifford", "rand_majorana_03"):
+    for name in ("cfg1_chain", "cfg1_chain_unbatched", "ref_mixed_clifford", "rand_majorana_03", "rand_majorana_07",
+                 "hubbard_3x3", "hubbard_6x6_3steps"):
         fx = load(name)
         run_gpu(fx)
         p = _native.context(0).profile()
