@@ -95,8 +95,8 @@ class Hubbard:
     metric = "term-gate applications/s (6x6 Fermi-Hubbard Majorana, 10 steps, deg<=6, tau=1e-7)"
     kind = "majorana"
     bytes_per_term = 24 + 16  # 3 words of Majorana bits + complex FP64 coefficient
-    kernel = "persistent per-gate kernel (pass_mrot, threshold after every gate)"
-    launch_unit = "one persistent run"
+    kernel = "Majorana batch-orbit path (morbit_*) + persistent per-gate kernel for the first gate"
+    launch_unit = "one commuting run (orbit batch)"
     steps = 10
     cpu_steps = 6
     params = dict(has_maxdegree=1, maxdegree=6, mincoeff=1e-7, deterministic=0)
