@@ -57,7 +57,7 @@ EXPORTS = ["ffg_create", "ffg_destroy", "ffg_last_error", "ffg_set_profiling", "
            "ffg_result_qubit_state", "ffg_result_fock_state", "ffg_result_free", "ffg_abs_le",
            "ffg_pauli_schedule", "ffg_stream", "ffg_pauli_rotations_noalloc",
            "ffg_pauli_propagate_batched", "ffg_batch_size", "ffg_batch_copy", "ffg_batch_adjoint",
-           "ffg_batch_free"]
+           "ffg_batch_free", "ffg_majorana_to_pauli", "ffg_result_sparse"]
 
 
 def lib():
@@ -104,6 +104,8 @@ def lib():
             L.ffg_batch_copy.argtypes = [vp, vp, vp, vp]
             L.ffg_batch_adjoint.argtypes = [vp, vp, vp, vp]
             L.ffg_batch_free.argtypes = [vp]
+            L.ffg_majorana_to_pauli.argtypes = [vp, vp, vp, vp, sz, ctypes.c_int, ctypes.POINTER(vp)]
+            L.ffg_result_sparse.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, sz, ctypes.POINTER(sz)]
             L.ffg_pauli_schedule.restype = i64
             L.ffg_pauli_schedule.argtypes = [vp, sz, ctypes.c_int, vp, i64]
             _lib = L
@@ -206,6 +208,16 @@ class Context:
                                                       _ptr(expect), ctypes.byref(out)))
         return expect, Batch(self, out, ninst, int(np.sum(gates["kind"] == ROT)), re.size)
 
+    def majorana_to_pauli(self, keys, re, im):
+        """Jordan-Wigner map of Majorana terms (host arrays) to a Pauli Result."""
+        keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
+        re = np.ascontiguousarray(re, dtype=np.float64)
+        im = None if im is None else np.ascontiguousarray(im, dtype=np.float64)
+        out = ctypes.c_void_p()
+        self.check(self.L.ffg_majorana_to_pauli(self.h, _ptr(keys), _ptr(re), _ptr(im), re.size, 0,
+                                                ctypes.byref(out)))
+        return Result(self, out)
+
     def __del__(self):
         if getattr(self, "h", None) and self.h.value:
             self.L.ffg_destroy(self.h)
@@ -280,6 +292,21 @@ class Result:
     def fock_state(self, b0=0, b1=0):
         b = np.array([b0, b1], dtype=np.uint64)
         return self._pair(self.ctx.L.ffg_result_fock_state, _ptr(b))
+
+    def sparse(self, n):
+        """(indptr, indices, data) of the 2^n x 2^n CSC matrix (Pauli results)."""
+        indptr = np.zeros((1 << n) + 1, dtype=np.int64)
+        nnz = ctypes.c_size_t(0)
+        L = self.ctx.L
+        self.ctx.check(L.ffg_result_sparse(self.h, int(n), _ptr(indptr), None, None, None, 0, ctypes.byref(nnz)))
+        m = nnz.value
+        indices = np.zeros(m, dtype=np.int64)
+        re = np.zeros(m)
+        im = np.zeros(m)
+        if m:
+            self.ctx.check(L.ffg_result_sparse(self.h, int(n), _ptr(indptr), _ptr(indices), _ptr(re), _ptr(im),
+                                               m, ctypes.byref(nnz)))
+        return indptr, indices, re + 1j * im
 
     def free(self):
         if self.h is not None and self.h.value:

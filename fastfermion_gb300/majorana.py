@@ -437,3 +437,19 @@ def majoranas(n):
 
 __all__ = ["MajoranaString", "MajoranaPolynomial", "MROT", "FockState", "majoranas",
            "MAX_MAJORANAS"]
+
+
+def jw(x):
+    """Jordan-Wigner map of a MajoranaString or MajoranaPolynomial to a
+    PauliPolynomial, computed on the GPU (src/transforms.h:124-151; the
+    reference binds it as ``jw``).  Index 2j maps to Z_0...Z_{j-1} X_j and 2j+1
+    to Z_0...Z_{j-1} Y_j; terms whose coefficient maps to exactly zero are
+    dropped."""
+    from . import _native
+    from .pauli import PauliPolynomial
+    if isinstance(x, MajoranaString):
+        x = MajoranaPolynomial(x)
+    if not isinstance(x, MajoranaPolynomial):
+        raise TypeError("jw(): expected a MajoranaString or MajoranaPolynomial")
+    keys, re, im = x.arrays()
+    return PauliPolynomial._from_result(_native.context().majorana_to_pauli(keys, re, im))

@@ -295,6 +295,24 @@ class PauliPolynomial:
                 r += c
         return r
 
+    def sparse(self, n=None, nup=None):
+        """The 2^n x 2^n matrix as a scipy.sparse.csc_matrix, built on the GPU
+        (src/pauli/sparse.h:20-131; n defaults to the extent).  The
+        fixed-particle-number subspace (nup) is not provided."""
+        if nup is not None:
+            raise NotImplementedError("sparse(n, nup): the subspace variant is not provided")
+        import scipy.sparse as sp
+
+        n = self.extent() if n is None else int(n)
+        if self._dev is not None:
+            res = self._dev
+        else:
+            keys, re, im = self.arrays()
+            from .propagation import propagate
+            res = propagate([], PauliPolynomial.from_arrays(keys, re, im))._dev
+        indptr, indices, data = res.sparse(n)
+        return sp.csc_matrix((data, indices, indptr), shape=(1 << n, 1 << n))
+
     def coefficient(self, s):
         if not isinstance(s, PauliString):
             s = PauliString(s)

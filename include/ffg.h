@@ -162,6 +162,30 @@ int ffg_result_fock_state(const ffg_result* r, const uint64_t* b /* [2] */, doub
 void ffg_result_free(ffg_result* r);
 
 /* -------------------------------------------------------------------------- */
+/* Conversions of polynomials, computed on the GPU.
+ *
+ * ffg_majorana_to_pauli: Jordan-Wigner map of a Majorana polynomial
+ * (keys [4][n] Majorana bits, re/im; host or device pointers as in
+ * ffg_pauli_propagate) to a Pauli polynomial result; terms whose mapped
+ * coefficient is exactly zero are dropped.  Replaces jordan_wigner /
+ * majorana_to_pauli, src/transforms.h:124-151, bound as `jw` in
+ * src/python_bind.cpp:172-175.
+ *
+ * ffg_result_sparse: the 2^n x 2^n CSC matrix of a Pauli result (qubit 0 is
+ * the most significant bit of the row/column index; qubits >= n are ignored),
+ * 0 <= n <= 30.  indptr has 2^n + 1 entries and is always written, with *nnz;
+ * indices/data_re/data_im (capacity cap) are written when they are non-NULL
+ * and cap >= *nnz (call once with indices = NULL to size them).  Within a
+ * column the entries come in increasing order of the bit-reversed X mask, as
+ * in the reference.  Replaces PauliPolynomial::sparse, src/pauli/sparse.h:20-131
+ * (bound in src/python_bind.cpp:127-140; the fixed-particle-number subspace
+ * variant is not provided). */
+int ffg_majorana_to_pauli(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im, size_t n,
+                          int on_device, ffg_result** out);
+int ffg_result_sparse(const ffg_result* r, int n, int64_t* indptr, int64_t* indices, double* data_re,
+                      double* data_im, size_t cap, size_t* nnz);
+
+/* -------------------------------------------------------------------------- */
 /* Batched instances and gradients.  No counterpart in the reference: its
  * propagate runs one observable through one circuit and has no derivatives.
  *

@@ -139,3 +139,102 @@ def majorana_propagate(gates, keys, re, im=None, maxdegree=None, mincoeff=0.0):
 
 def ffo_abs(re, im):
     return lib().ffo_abs(float(re), float(im))
+
+
+# ---------------------------------------------------------------------------
+# Conversions (pure Python restatements; small inputs only)
+# ---------------------------------------------------------------------------
+
+def _popc(v):
+    return bin(v).count("1")
+
+
+def _ipow(m):
+    return (1 + 0j, 1j, -1 + 0j, -1j)[m % 4]
+
+
+def jordan_wigner(keys, re, im=None):
+    """Jordan-Wigner map of Majorana terms (keys (4, n), re, im) to Pauli terms
+    (src/transforms.h:124-151): index i = 2j + r maps to Z_0..Z_{j-1} X_j (r = 0)
+    or Z_0..Z_{j-1} Y_j (r = 1), multiplied in increasing index order with the
+    phase bookkeeping of pauli_string_multiply (src/pauli/algebra.h:227-233);
+    coefficient v * i^jpow; exact zeros dropped (compress(0)).  Returns
+    (keys (4, m) uint64, re, im) in input order."""
+    keys = np.asarray(keys, dtype=np.uint64).reshape(4, -1)
+    re = np.asarray(re, dtype=np.float64)
+    im = np.zeros_like(re) if im is None else np.asarray(im, dtype=np.float64)
+    ok, ore, oim = [], [], []
+    for t in range(re.size):
+        a = sum(int(keys[w, t]) << (64 * w) for w in range(4))
+        x = z = 0
+        jpow = 0
+        i = 0
+        while a >> i:
+            if (a >> i) & 1:
+                j, r = divmod(i, 2)
+                bx = 1 << j
+                bz = (1 << (j + r)) - 1
+                jpow += _popc(x & z) + _popc(bx & bz) + 2 * _popc(z & bx)
+                x ^= bx
+                z ^= bz
+                jpow -= _popc(x & z)
+            i += 1
+        v = complex(re[t], im[t])
+        p = _ipow(jpow)
+        c = complex(v.real * p.real - v.imag * p.imag, v.real * p.imag + v.imag * p.real)
+        c = complex(0.0 + c.real, 0.0 + c.imag)
+        if c.real == 0.0 and c.imag == 0.0:
+            continue
+        m64 = (1 << 64) - 1
+        ok.append([x & m64, x >> 64, z & m64, z >> 64])
+        ore.append(c.real)
+        oim.append(c.imag)
+    k = np.array(ok, dtype=np.uint64).T.reshape(4, -1) if ok else np.zeros((4, 0), dtype=np.uint64)
+    return k, np.array(ore), np.array(oim)
+
+
+def pauli_sparse(keys, re, im, n):
+    """CSC arrays (indptr, indices, data) of the 2^n x 2^n matrix of a Pauli
+    polynomial (src/pauli/sparse.h:20-131): qubit q maps to bit n-1-q of the
+    basis index (qubits >= n ignored); terms grouped by the flipped X mask in
+    increasing order; column b gets, per group, the entry at row b ^ xf with
+    value sum_t (-1)^|b & zf_t| i^{#Y_t} c_t when it is not zero.  Ties inside a
+    group are summed in increasing flipped-Z order."""
+    keys = np.asarray(keys, dtype=np.uint64).reshape(4, -1)
+
+    def flip(v):
+        r = 0
+        for q in range(n):
+            if (v >> q) & 1:
+                r |= 1 << (n - 1 - q)
+        return r
+    mask = (1 << n) - 1
+    terms = []
+    for t in range(keys.shape[1]):
+        x0, x1, z0, z1 = (int(keys[w, t]) for w in range(4))
+        ny = _popc(x0 & z0) + _popc(x1 & z1)
+        p = _ipow(ny)
+        v = complex(re[t], im[t])
+        c = complex(p.real * v.real - p.imag * v.imag, p.real * v.imag + p.imag * v.real)
+        terms.append((flip(x0 & mask), flip(z0 & mask), c))
+    terms.sort(key=lambda u: (u[0], u[1]))
+    groups = []
+    for xf, zf, c in terms:
+        if groups and groups[-1][0] == xf:
+            groups[-1][1].append((zf, c))
+        else:
+            groups.append((xf, [(zf, c)]))
+    indptr = [0]
+    indices, data = [], []
+    for b in range(1 << n):
+        for xf, members in groups:
+            sr = si = 0.0
+            for zf, c in members:
+                sg = -1.0 if _popc(b & zf) & 1 else 1.0
+                sr += sg * c.real
+                si += sg * c.imag
+            if sr != 0.0 or si != 0.0:
+                indices.append(b ^ xf)
+                data.append(complex(sr, si))
+        indptr.append(len(indices))
+    return np.array(indptr, dtype=np.int64), np.array(indices, dtype=np.int64), np.array(data, dtype=complex)

@@ -423,6 +423,33 @@ def hea_cases(ff):
     yield "hea_shift_70q", lambda: shift("hea_shift_70q", 70, 2, 2, 9, 3, True)
 
 
+def transform_cases(ff):
+    """Jordan-Wigner maps of random Majorana polynomials and sparse matrices of
+    Pauli polynomials, by the reference (kinds "jw" and "sparse")."""
+    rng = np.random.default_rng(777)
+
+    def jw_case(nm, modes, nterms, dmax):
+        p = random_maj_poly(ff, rng, modes, nterms, dmax)
+        ok, ore, oim = poly_arrays(p, "majorana")
+        res = ff.jw(p)
+        rk, rre, rim = poly_arrays(res, "pauli")
+        save(nm, kind="jw", obs_keys=ok, obs_re=ore, obs_im=oim, res_keys=rk, res_re=rre, res_im=rim)
+        print(f"{nm:32s} terms={len(res):8d}", flush=True)
+    yield "jw_small", lambda: jw_case("jw_small", list(range(12)), 40, 5)
+    yield "jw_wide", lambda: jw_case("jw_wide", [0, 1, 62, 63, 64, 65, 127, 128, 129, 200, 201, 254, 255], 60, 6)
+
+    def sparse_case(nm, poly, n):
+        ok, ore, oim = poly_arrays(poly, "pauli")
+        m = poly.sparse(n)
+        save(nm, kind="sparse", n=n, obs_keys=ok, obs_re=ore, obs_im=oim, indptr=m.indptr.astype(np.int64),
+             indices=m.indices.astype(np.int64), data=np.asarray(m.data, dtype=complex))
+        print(f"{nm:32s} nnz={m.nnz:8d}", flush=True)
+    yield "sparse_random6", lambda: sparse_case("sparse_random6", random_pauli_poly(ff, rng, list(range(6)), 40, True, 4), 6)
+    yield "sparse_propagated", lambda: sparse_case(
+        "sparse_propagated", ff.propagate(tfim(ff, 6, 0.1) * 5, ff.PauliString("Z" + "I" * 5)), 6)
+    yield "sparse_dropped_qubits", lambda: sparse_case("sparse_dropped_qubits", random_pauli_poly(ff, rng, list(range(7)), 25, True, 3), 5)
+
+
 REF = "/root/reference"
 
 if __name__ == "__main__":
@@ -432,7 +459,7 @@ if __name__ == "__main__":
     a = ap.parse_args()
     REF = a.ref
     ff = load_reference(REF)
-    for name, fn in list(cases(ff)) + list(hea_cases(ff)):
+    for name, fn in list(cases(ff)) + list(hea_cases(ff)) + list(transform_cases(ff)):
         if a.only and a.only not in name:
             continue
         fn()
