@@ -2904,8 +2904,11 @@ int ffg_result_sparse(const ffg_result* r, int n, int64_t* indptr, int64_t* indi
         }
         std::vector<size_t> ord(m);
         for (size_t t = 0; t < m; t++) ord[t] = t;
+        // (xf, zf, position): equal masks (qubits >= n dropped) keep term order
         std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
-            return xf[a] != xf[b] ? xf[a] < xf[b] : zf[a] < zf[b];
+            if (xf[a] != xf[b]) return xf[a] < xf[b];
+            if (zf[a] != zf[b]) return zf[a] < zf[b];
+            return a < b;
         });
         std::vector<u64> gxf, szf(m);
         std::vector<u32> gstart;

@@ -199,7 +199,7 @@ def pauli_sparse(keys, re, im, n):
     basis index (qubits >= n ignored); terms grouped by the flipped X mask in
     increasing order; column b gets, per group, the entry at row b ^ xf with
     value sum_t (-1)^|b & zf_t| i^{#Y_t} c_t when it is not zero.  Ties inside a
-    group are summed in increasing flipped-Z order."""
+    group are summed in increasing flipped-Z order, then term order."""
     keys = np.asarray(keys, dtype=np.uint64).reshape(4, -1)
 
     def flip(v):
