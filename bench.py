@@ -8,12 +8,14 @@ One step = the whole theta_h sweep (7 propagations).  Term-gate applications
 ("apps") = sum over rotation gates of the live terms entering the gate.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload kicked_ising|hubbard|hea]
+                    [--workload kicked_ising|kicked_ising_w10|hubbard|hea]
 
 --workload hubbard measures the 6x6 Fermi-Hubbard Majorana propagation (144
 Majoranas, 10 Trotter steps, degree <= 6, tau = 1e-7) instead; one step = one
 propagation.  --workload hea measures 256 instances of a 50-qubit ansatz in one
-batched propagation plus the adjoint gradient of every angle.
+batched propagation plus the adjoint gradient of every angle.  --workload
+kicked_ising_w10 runs the kicked-Ising circuit at maximum weight 10 (theta_h =
+0.3), the large-N case with ~4e8 terms inside a batch at the peak.
 
 Prints one JSON line on rank 0.  Multi-GPU runs are independent replicas (the
 propagation of one observable does not shard without a per-gate exchange):
@@ -47,12 +49,17 @@ class KickedIsing:
     kernel = "orbit engine (orbit_classify..orbit_process_big) + persistent per-gate kernel"
     launch_unit = "one commuting run (orbit batch) or one persistent run"
     thetas = (0.1, 0.3, 0.5, 0.7, 0.9, 1.1, math.pi / 2)
-    params = dict(maxdegree=MAXDEG, topk=0, mincoeff=TAU, max_xweight=-1, xtrunc_period=1,
-                  batched=1, deterministic=0)
+    maxdeg = MAXDEG
+    cpu_steps = 20  # Trotter steps of each propagation in the CPU sample
 
-    def tables(self):
+    @property
+    def params(self):
+        return dict(maxdegree=self.maxdeg, topk=0, mincoeff=TAU, max_xweight=-1, xtrunc_period=1,
+                    batched=1, deterministic=0)
+
+    def tables(self, steps=20):
         import fastfermion_gb300 as ff
-        return [ff.encode_pauli_circuit(ff.build_circuit(ff.workloads.kicked_ising_circuit(th)))
+        return [ff.encode_pauli_circuit(ff.build_circuit(ff.workloads.kicked_ising_circuit(th, steps=steps)))
                 for th in self.thetas]
 
     def observable(self):
@@ -71,21 +78,34 @@ class KickedIsing:
         sweep, repeated until min_seconds of CPU time have passed."""
         from oracle import oracle as O
         keys, re, im = self.observable()
+        if self.cpu_steps != 20:
+            tabs = self.tables(self.cpu_steps)
         apps, sweeps = 0, 0
         t0 = time.perf_counter()
         while sweeps == 0 or time.perf_counter() - t0 < min_seconds:
             for tab in tabs:
-                apps += O.pauli_propagate(tab, keys, re, im, maxdegree=MAXDEG, mincoeff=TAU,
+                apps += O.pauli_propagate(tab, keys, re, im, maxdegree=self.maxdeg, mincoeff=TAU,
                                           n_threads=cores).apps
             sweeps += 1
+        part = "" if self.cpu_steps == 20 else f" (first {self.cpu_steps} of 20 Trotter steps)"
         return apps, time.perf_counter() - t0, cores, (
-            f"{sweeps} x the full theta_h sweep of the same workload, sharded OpenMP port "
+            f"{sweeps} x the theta_h sweep of the same workload{part}, sharded OpenMP port "
             "of the reference algorithm")
 
     def config(self):
         return {"workload": self.name, "lattice": "10x10 open", "trotter_steps": 20,
-                "maxdegree": MAXDEG, "mincoeff": TAU, "theta_h": [round(t, 6) for t in self.thetas],
+                "maxdegree": self.maxdeg, "mincoeff": TAU, "theta_h": [round(t, 6) for t in self.thetas],
                 "observable": "Z_55", "batched": True}
+
+
+class KickedIsingW10(KickedIsing):
+    """The same circuit at maximum weight 10, theta_h = 0.3: the large-N case
+    (about 4e8 terms inside a batch at the peak, 2e11 apps per propagation)."""
+    name = "kicked_ising_10x10_w10_tau1e-6"
+    metric = "term-gate applications/s (10x10 kicked Ising, 20 steps, W=10, tau=1e-6, theta_h=0.3)"
+    thetas = (0.3,)
+    maxdeg = 10
+    cpu_steps = 10
 
 
 class Hubbard:
@@ -188,7 +208,8 @@ class BatchedAnsatz:
                 "checkpoint_every": 1}
 
 
-WORKLOADS = {"kicked_ising": KickedIsing, "hubbard": Hubbard, "hea": BatchedAnsatz}
+WORKLOADS = {"kicked_ising": KickedIsing, "kicked_ising_w10": KickedIsingW10, "hubbard": Hubbard,
+             "hea": BatchedAnsatz}
 
 
 def parse():

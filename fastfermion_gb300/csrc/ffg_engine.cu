@@ -176,6 +176,7 @@ struct ffg_ctx {
     int orbit_route_big = 8;    // |A| from which a group skips the warp-level pass (FFG_ORBIT_ROUTE)
     bool orbit_team = true;     // 256-thread team pass before the 1024-thread pass (FFG_ORBIT_TEAM=0 disables)
     bool morbit = true;         // batch-orbit path for commuting Majorana runs (FFG_MORBIT=0 disables)
+    bool pdl = true;            // programmatic dependent launch of the orbit kernels (FFG_PDL=0 disables)
     int morbit_min_gates = 2;   // shortest Majorana run sent to the batch-orbit path
     MBatchGate* d_mgates = nullptr;
     size_t mgates_cap = 0;
@@ -297,6 +298,27 @@ int grid_for(const ffg_ctx* ctx, u64 items) {
     u64 lim = (u64)ctx->num_sms * 8;
     if (b < 1) b = 1;
     return (int)std::min(b, lim);
+}
+
+// Kernel launch that may start while the previous kernel on the stream is
+// finishing (programmatic dependent launch): the kernel's blocks are scheduled
+// early and wait in griddepcontrol.wait (wait_prior_grid) until the previous
+// grid has completed.  Every kernel launched this way calls wait_prior_grid
+// before touching memory.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_k(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
 }
 
 // ---------------------------------------------------------------------------
@@ -849,19 +871,19 @@ struct Engine {
             // sc.big -> retry_list (count nretry[0]) -> sc.big (count nretry[1])
             bp.retry = retry_list;
             bp.nretry = nretry;
-            orbit_process_big<NWo, CPLX, true, 256, kTeamCap><<<ctx->num_sms * team_per_sm, 256, tt, ctx->stream>>>(
-                in, out, sc, oc, a, bp, sc.big, 0, nbig_dev);
+            CK(launch_k(ctx->pdl, orbit_process_big<NWo, CPLX, true, 256, kTeamCap>, ctx->num_sms * team_per_sm, 256,
+                        tt, ctx->stream, in, out, sc, oc, a, bp, (const u32*)sc.big, 0u, nbig_dev));
             bp.retry = sc.big;
             bp.nretry = nretry + 1;
-            orbit_process_big<NWo, CPLX, true><<<ctx->num_sms, 1024, tb, ctx->stream>>>(
-                in, out, sc, oc, a, bp, retry_list, 0, nretry);
+            CK(launch_k(ctx->pdl, orbit_process_big<NWo, CPLX, true>, ctx->num_sms, 1024, tb, ctx->stream, in, out, sc,
+                        oc, a, bp, (const u32*)retry_list, 0u, (const u32*)nretry));
             ctx->prof.kernel_launches += 2;
         } else {
             // sc.big -> retry_list (count nretry[1])
             bp.retry = retry_list;
             bp.nretry = nretry + 1;
-            orbit_process_big<NWo, CPLX, true><<<ctx->num_sms, 1024, tb, ctx->stream>>>(
-                in, out, sc, oc, a, bp, sc.big, 0, nbig_dev);
+            CK(launch_k(ctx->pdl, orbit_process_big<NWo, CPLX, true>, ctx->num_sms, 1024, tb, ctx->stream, in, out, sc,
+                        oc, a, bp, (const u32*)sc.big, 0u, nbig_dev));
             ctx->prof.kernel_launches++;
         }
         OSTEP("orbit_process_big");
@@ -1025,17 +1047,19 @@ struct Engine {
                     OrbitCounters* oc = ctx->d_ocw + j;
                     const StoreView& in = S[j & 1].v;
                     const StoreView& out = S[(j + 1) & 1].v;
-                    orbit_gate<<<1, 32, 0, ctx->stream>>>(oc, j ? oc - 1 : nullptr, n_cur, sc.gmask + 1, nretry);
-                    orbit_classify<NWo, CPLX><<<G, kBlock, 0, ctx->stream>>>(in, out, sc, oc, a);
+                    const bool pdl = ctx->pdl;
+                    const OrbitCounters* prev = j ? oc - 1 : nullptr;
+                    CK(launch_k(pdl, orbit_gate, 1, 32, 0, ctx->stream, oc, prev, n_cur, sc.gmask + 1, nretry));
+                    CK(launch_k(pdl, orbit_classify<NWo, CPLX>, G, kBlock, 0, ctx->stream, in, out, sc, oc, a));
                     OSTEP("orbit_classify");
-                    orbit_group<KW><<<G, kBlock, 0, ctx->stream>>>(sc, oc);
+                    CK(launch_k(pdl, orbit_group<KW>, G, kBlock, 0, ctx->stream, sc, oc));
                     OSTEP("orbit_group");
-                    orbit_offsets<<<G, kBlock, 0, ctx->stream>>>(sc, oc);
+                    CK(launch_k(pdl, orbit_offsets, G, kBlock, 0, ctx->stream, sc, oc));
                     OSTEP("orbit_offsets");
-                    orbit_scatter<<<G, kBlock, 0, ctx->stream>>>(sc, oc);
+                    CK(launch_k(pdl, orbit_scatter, G, kBlock, 0, ctx->stream, sc, (const OrbitCounters*)oc));
                     OSTEP("orbit_scatter");
-                    orbit_process<NWo, CPLX><<<ctx->num_sms * 2, 32 * kOrbitWarps, smem, ctx->stream>>>(in, out, sc,
-                                                                                                     oc, a);
+                    CK(launch_k(pdl, orbit_process<NWo, CPLX>, ctx->num_sms * 2, 32 * kOrbitWarps, smem, ctx->stream,
+                                in, out, sc, oc, a));
                     OSTEP("orbit_process");
                     ctx->prof.kernel_launches += 6;
                     rc = launch_big_tiers(in, out, sc, a, oc);
@@ -2073,6 +2097,7 @@ int ffg_create(ffg_ctx** out, int device) {
     if (const char* d = getenv("FFG_ORBIT_ROUTE")) ctx->orbit_route_big = std::max(1, atoi(d));
     if (const char* d = getenv("FFG_ORBIT_TEAM")) ctx->orbit_team = atoi(d) != 0;
     if (const char* d = getenv("FFG_MORBIT")) ctx->morbit = atoi(d) != 0;
+    if (const char* d = getenv("FFG_PDL")) ctx->pdl = atoi(d) != 0;
     if (const char* d = getenv("FFG_MORBIT_MIN")) ctx->morbit_min_gates = std::max(1, atoi(d));
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);

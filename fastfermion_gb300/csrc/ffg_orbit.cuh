@@ -113,6 +113,10 @@ struct OrbitBatchArgs {
     u64 inst_mask;
 };
 
+// Waits until the grid this one depends on (programmatic dependent launch)
+// has completed and its memory is visible; returns at once for a normal launch.
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // barrier of a team of TEAM threads (a warp, or the whole block)
 template <int TEAM>
 __device__ __forceinline__ void team_sync() {
@@ -179,6 +183,7 @@ __device__ __forceinline__ void out_append(const StoreView& o, OrbitCounters* oc
 // batch left it.
 __global__ void orbit_gate(OrbitCounters* cur, const OrbitCounters* prev, u64 n_first, u64 gslots_cap,
                            u32* nretry) {
+    wait_prior_grid();
     constexpr u32 nw = sizeof(OrbitCounters) / 4;
     for (u32 i = threadIdx.x; i < nw; i += blockDim.x) ((u32*)cur)[i] = 0;
     __syncwarp();
@@ -208,6 +213,7 @@ __global__ void orbit_gate(OrbitCounters* cur, const OrbitCounters* prev, u64 n_
 template <int NW, bool CPLX>
 __global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, StoreView out, OrbitScratch sc,
                                                          OrbitCounters* oc, OrbitBatchArgs a) {
+    wait_prior_grid();
     constexpr int KW = 2 * NW;
     if (*(volatile u32*)&oc->skip) return;
     const u64 n_in = *(volatile u64*)&oc->n_in;
@@ -276,6 +282,7 @@ __device__ __forceinline__ bool same_group(const OrbitScratch& sc, u64 i, u64 j)
 // representative of each term's group: the term that claims the index slot
 template <int KW>
 __global__ void __launch_bounds__(kBlock) orbit_group(OrbitScratch sc, OrbitCounters* oc) {
+    wait_prior_grid();
     if (*(volatile u32*)&oc->skip) return;
     const u64 n_in = *(volatile u64*)&oc->n_in;
     const u64 gmask = *(volatile u64*)&oc->gmask;
@@ -318,6 +325,7 @@ __global__ void __launch_bounds__(kBlock) orbit_group(OrbitScratch sc, OrbitCoun
 // placement of the groups works (each group is processed on its own), so the
 // ranges come from warp-aggregated atomic additions, in parallel.
 __global__ void __launch_bounds__(kBlock) orbit_offsets(OrbitScratch sc, OrbitCounters* oc) {
+    wait_prior_grid();
     if (*(volatile u32*)&oc->skip) return;
     const u32 ng = *(volatile u32*)&oc->ngroups;
     const int lane = threadIdx.x & 31;
@@ -342,6 +350,7 @@ __global__ void __launch_bounds__(kBlock) orbit_offsets(OrbitScratch sc, OrbitCo
 }
 
 __global__ void __launch_bounds__(kBlock) orbit_scatter(OrbitScratch sc, const OrbitCounters* oc) {
+    wait_prior_grid();
     if (*(volatile const u32*)&oc->skip) return;
     const u64 n_in = *(volatile const u64*)&oc->n_in;
     const u64 stride = (u64)gridDim.x * blockDim.x;
@@ -410,6 +419,7 @@ __device__ __forceinline__ void table_insert(OrbitTable<KW, CPLX>& T, const u64*
 template <int NW, bool CPLX>
 __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, StoreView out, OrbitScratch sc,
                                                                   OrbitCounters* oc, OrbitBatchArgs a) {
+    wait_prior_grid();
     constexpr int KW = 2 * NW;
     extern __shared__ unsigned char smem[];
     OrbitTable<KW, CPLX>* tables = (OrbitTable<KW, CPLX>*)smem;
@@ -659,6 +669,7 @@ template <int NW, bool CPLX, bool SM, int TB = 1024, u32 CAP = kBlockCap>
 __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView out, OrbitScratch sc,
                                                           OrbitCounters* oc, OrbitBatchArgs a, BigPool bp,
                                                           const u32* list, u32 nlist, const u32* nlist_dev) {
+    wait_prior_grid();
     constexpr int KW = 2 * NW;
     __shared__ long long red[3][32];
     extern __shared__ __align__(16) unsigned char btab[];

@@ -298,6 +298,10 @@ def cases(ff):
         yield nm, (lambda nm=nm, th=th: pauli_case(
             ff, nm, [mk(ff, s) for s in W.kicked_ising_circuit(th)], P([(55, "Z")]),
             maxdegree=8, mincoeff=1e-6))
+    # the large-N variant: W = 10 (peak ~4e8 terms inside a batch; ~15 min on 8 cores)
+    yield "cfg2w10_kicked_ising_0p3000", lambda: pauli_case(
+        ff, "cfg2w10_kicked_ising_0p3000", [mk(ff, s) for s in W.kicked_ising_circuit(0.3)], P([(55, "Z")]),
+        maxdegree=10, mincoeff=1e-6, n_threads=os.cpu_count(), parallel="sharded")
     # smaller kicked-Ising variants with large in-batch growth
     yield "ki_6x6_w6", lambda: pauli_case(ff, "ki_6x6_w6", [mk(ff, s) for s in W.kicked_ising_circuit(0.7, 6, 6, 8)], P([(21, "Z")]), maxdegree=6, mincoeff=1e-5)
     yield "ki_8x8_w6_unbatched", lambda: pauli_case(ff, "ki_8x8_w6_unbatched", [mk(ff, s) for s in W.kicked_ising_circuit(0.4, 8, 8, 6)], P([(27, "Z")]), maxdegree=6, mincoeff=1e-5, batched=False)
