@@ -177,9 +177,12 @@ struct ffg_ctx {
     bool orbit_team = true;     // 256-thread team pass before the 1024-thread pass (FFG_ORBIT_TEAM=0 disables)
     bool morbit = true;         // batch-orbit path for commuting Majorana runs (FFG_MORBIT=0 disables)
     bool pdl = true;            // programmatic dependent launch of the orbit kernels (FFG_PDL=0 disables)
+    bool orbit_qidx = true;     // classify against the gates on each term's support (FFG_ORBIT_QIDX=0 disables)
     int morbit_min_gates = 2;   // shortest Majorana run sent to the batch-orbit path
     MBatchGate* d_mgates = nullptr;
     size_t mgates_cap = 0;
+    u32* d_qidx = nullptr;      // qubit -> gate indexes of the orbit batches of a window call
+    size_t qidx_cap = 0;
     BatchGate* d_bgates = nullptr;
     size_t bgates_cap = 0;
     char* d_oscratch = nullptr;
@@ -1023,6 +1026,22 @@ struct Engine {
             attr_set = true;
         }
         const int G = ctx->num_sms * 8;
+        // qubit -> gate indexes of every job (Pauli batches), uploaded once
+        std::vector<size_t> qbase(njobs, 0);
+        if (PAULI && !h_bgates.empty()) {
+            std::vector<u32> qv;
+            for (int j = 0; j < njobs; j++) {
+                qbase[j] = qv.size();
+                build_qidx(jobs[j].g0, jobs[j].k, qv);
+            }
+            int rc = upload(ctx->d_qidx, ctx->qidx_cap, qv);
+            if (rc) return rc;
+        }
+        auto args_of = [&](int j) {
+            OrbitBatchArgs a = batch_args(jobs[j], maxdeg);
+            if (PAULI && !h_bgates.empty() && ctx->orbit_qidx) a.qidx = ctx->d_qidx + qbase[j];
+            return a;
+        };
         int i = 0, regrows = 0;
         u64 grow = 0;
         while (i < njobs) {
@@ -1043,7 +1062,7 @@ struct Engine {
             {
                 PhaseScope ps(ctx, PH_ROT);
                 for (int j = 0; j < m; j++) {
-                    const OrbitBatchArgs a = batch_args(jobs[i + j], maxdeg);
+                    const OrbitBatchArgs a = args_of(i + j);
                     OrbitCounters* oc = ctx->d_ocw + j;
                     const StoreView& in = S[j & 1].v;
                     const StoreView& out = S[(j + 1) & 1].v;
@@ -1092,7 +1111,7 @@ struct Engine {
                 if (oc.skip) break;
                 const bool last = j == m - 1 || ctx->h_ocw[j + 1].skip;
                 if (last && nleft) {
-                    const OrbitBatchArgs a = batch_args(jobs[i + j], maxdeg);
+                    const OrbitBatchArgs a = args_of(i + j);
                     const int br = finish_big_groups(S[j & 1].v, S[(j + 1) & 1].v, sc, a, nleft, ctx->d_ocw + j, &oc);
                     if (br < 0) return br;
                     if (br == 2) {
@@ -1350,7 +1369,35 @@ struct Engine {
             gate_of_op[o] = (int)bg.size();
             bg.push_back(b);
         }
+        h_bgates = bg;
         return upload(ctx->d_bgates, ctx->bgates_cap, bg);
+    }
+
+    std::vector<BatchGate> h_bgates;  // host copy of the batch gate table
+
+    // qubit -> gate index of batch gates [g0, g0 + k) (layout of OrbitBatchArgs::qidx)
+    void build_qidx(int g0, int k, std::vector<u32>& out) const {
+        std::vector<std::vector<u32>> lists(128);
+        for (int t = 0; t < k; t++) {
+            const BatchGate& G = h_bgates[g0 + t];
+            for (int w = 0; w < NW; w++) {
+                u64 sup = G.p[w] | G.p[NW + w];
+                while (sup) {
+                    const int q = 64 * w + __builtin_ctzll(sup);
+                    sup &= sup - 1;
+                    lists[q].push_back((u32)t);
+                }
+            }
+        }
+        const size_t base = out.size();
+        out.resize(base + 129);
+        u32 e = 0;
+        for (int q = 0; q < 128; q++) {
+            out[base + q] = e;
+            e += (u32)lists[q].size();
+        }
+        out[base + 128] = e;
+        for (int q = 0; q < 128; q++) out.insert(out.end(), lists[q].begin(), lists[q].end());
     }
 
     // ---------------------------------------------------------------------
@@ -2098,6 +2145,7 @@ int ffg_create(ffg_ctx** out, int device) {
     if (const char* d = getenv("FFG_ORBIT_TEAM")) ctx->orbit_team = atoi(d) != 0;
     if (const char* d = getenv("FFG_MORBIT")) ctx->morbit = atoi(d) != 0;
     if (const char* d = getenv("FFG_PDL")) ctx->pdl = atoi(d) != 0;
+    if (const char* d = getenv("FFG_ORBIT_QIDX")) ctx->orbit_qidx = atoi(d) != 0;
     if (const char* d = getenv("FFG_MORBIT_MIN")) ctx->morbit_min_gates = std::max(1, atoi(d));
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
@@ -2138,6 +2186,7 @@ int ffg_destroy(ffg_ctx* ctx) {
     if (ctx->d_groups2) cudaFree(ctx->d_groups2);
     if (ctx->d_bgates) cudaFree(ctx->d_bgates);
     if (ctx->d_mgates) cudaFree(ctx->d_mgates);
+    if (ctx->d_qidx) cudaFree(ctx->d_qidx);
     if (ctx->d_oscratch) cudaFree(ctx->d_oscratch);
     if (ctx->bigpool.p) cudaFree(ctx->bigpool.p);
     if (ctx->d_oc) cudaFree(ctx->d_oc);

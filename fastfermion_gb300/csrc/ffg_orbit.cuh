@@ -111,6 +111,10 @@ struct OrbitBatchArgs {
     int inst_plane;
     int inst_shift;
     u64 inst_mask;
+    // qubit -> gates index of the batch (null: test every gate): gates touching
+    // qubit q are qidx[129 + qidx[q] .. 129 + qidx[q + 1]).  A Pauli gate
+    // anticommutes only with terms whose support it touches.
+    const u32* qidx;
 };
 
 // Waits until the grid this one depends on (programmatic dependent launch)
@@ -229,14 +233,39 @@ __global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, StoreView
         load_key<KW>(in, i, q);
         u64 A[kAW] = {};
         u64 U[KW] = {};
-        for (int t = 0; t < a.k; t++) {
-            u64 par = 0;
+        if (a.qidx) {
+            // candidates: the gates on the term's support
 #pragma unroll
-            for (int w = 0; w < NW; w++) par ^= (q[w] & gp[t][NW + w]) ^ (q[NW + w] & gp[t][w]);
-            if (__popcll(par) & 1) {
-                A[t >> 6] |= 1ull << (t & 63);
+            for (int ws = 0; ws < NW; ws++) {
+                u64 sup = q[ws] | q[NW + ws];
+                while (sup) {
+                    const int qb = 64 * ws + __ffsll((long long)sup) - 1;
+                    sup &= sup - 1;
+                    const u32 e1 = __ldg(&a.qidx[qb + 1]);
+                    for (u32 e = __ldg(&a.qidx[qb]); e < e1; e++) {
+                        const int t = (int)__ldg(&a.qidx[129 + e]);
+                        if ((A[t >> 6] >> (t & 63)) & 1ull) continue;
+                        u64 par = 0;
 #pragma unroll
-                for (int w = 0; w < KW; w++) U[w] |= gp[t][w];
+                        for (int w = 0; w < NW; w++) par ^= (q[w] & gp[t][NW + w]) ^ (q[NW + w] & gp[t][w]);
+                        if (__popcll(par) & 1) {
+                            A[t >> 6] |= 1ull << (t & 63);
+#pragma unroll
+                            for (int w = 0; w < KW; w++) U[w] |= gp[t][w];
+                        }
+                    }
+                }
+            }
+        } else {
+            for (int t = 0; t < a.k; t++) {
+                u64 par = 0;
+#pragma unroll
+                for (int w = 0; w < NW; w++) par ^= (q[w] & gp[t][NW + w]) ^ (q[NW + w] & gp[t][w]);
+                if (__popcll(par) & 1) {
+                    A[t >> 6] |= 1ull << (t & 63);
+#pragma unroll
+                    for (int w = 0; w < KW; w++) U[w] |= gp[t][w];
+                }
             }
         }
         bool any = false;
