@@ -944,7 +944,7 @@ struct Engine {
         OrbitScratch sc{};
         u64 hc = pow2_at_least(std::max<u64>(2 * cap_in, 1024));
         size_t need = align256((size_t)kAW * cap_in * 8) + align256((size_t)KW * cap_in * 8) +
-                      8 * align256(cap_in * 4) + align256(hc * 8) + 256;
+                      8 * align256(cap_in * 4) + align256(2 * cap_in * 8) + align256(hc * 8) + 256;
         if (ctx->oscratch_bytes < need) {
             if (ctx->d_oscratch && cudaFree(ctx->d_oscratch) != cudaSuccess) return sc;
             ctx->d_oscratch = nullptr;
@@ -975,6 +975,8 @@ struct Engine {
         p += align256(cap_in * 4);
         nretry = (u32*)p;
         p += 256;
+        sc.gcoef = (double*)p;
+        p += align256(2 * cap_in * 8);
         sc.gslots = (u64*)p;
         sc.gmask = hc - 1;
         sc.cap_in = cap_in;
@@ -1075,7 +1077,8 @@ struct Engine {
                     OSTEP("orbit_group");
                     CK(launch_k(pdl, orbit_offsets, G, kBlock, 0, ctx->stream, sc, oc));
                     OSTEP("orbit_offsets");
-                    CK(launch_k(pdl, orbit_scatter, G, kBlock, 0, ctx->stream, sc, (const OrbitCounters*)oc));
+                    CK(launch_k(pdl, orbit_scatter<KW, CPLX>, G, kBlock, 0, ctx->stream, in, sc,
+                                (const OrbitCounters*)oc));
                     OSTEP("orbit_scatter");
                     CK(launch_k(pdl, orbit_process<NWo, CPLX>, ctx->num_sms * 2, 32 * kOrbitWarps, smem, ctx->stream,
                                 in, out, sc, oc, a));
@@ -1228,7 +1231,7 @@ struct Engine {
                 OSTEP("morbit_classify");
                 orbit_group<KW><<<G, kBlock, 0, ctx->stream>>>(sc, oc);
                 orbit_offsets<<<G, kBlock, 0, ctx->stream>>>(sc, oc);
-                orbit_scatter<<<G, kBlock, 0, ctx->stream>>>(sc, oc);
+                orbit_scatter<KW, true><<<G, kBlock, 0, ctx->stream>>>(cur.v, sc, oc);
                 OSTEP("orbit_scatter");
                 morbit_single<KW><<<G, kBlock, 0, ctx->stream>>>(cur.v, dst.v, sc, oc, a);
                 OSTEP("morbit_single");
@@ -2053,7 +2056,7 @@ int batch_adjoint(ffg_batch* h, const double* weights, double* grad_theta, doubl
             orbit_classify<NW, false><<<g, kBlock, 0, ctx->stream>>>(in, dummy.v, sc, ctx->d_oc, a);
             orbit_group<KW><<<g, kBlock, 0, ctx->stream>>>(sc, ctx->d_oc);
             orbit_offsets<<<g, kBlock, 0, ctx->stream>>>(sc, ctx->d_oc);
-            orbit_scatter<<<g, kBlock, 0, ctx->stream>>>(sc, ctx->d_oc);
+            orbit_scatter<KW, false><<<g, kBlock, 0, ctx->stream>>>(in, sc, ctx->d_oc);
             adj_passthrough<KW><<<g, kBlock, 0, ctx->stream>>>(in, n_in, sc, A);
             adj_orbit_warp<NW><<<ctx->num_sms * 2, 32 * kAdjWarps, warp_smem, ctx->stream>>>(in, sc, ctx->d_oc, A);
             CK(cudaGetLastError());

@@ -206,15 +206,15 @@ __device__ bool mgroup(const StoreView& in, const StoreView& out, const OrbitScr
     }
     team_sync<TEAM>();
     for (u32 m = rank; m < m0; m += TEAM) {
-        const u32 i = sc.order[base + m];
+        const u64 pm = (u64)base + m;
         u64 k[KW];
 #pragma unroll
         for (int w = 0; w < KW; w++) {
-            k[w] = in.key[(u64)w * in.cap + i];
+            k[w] = sc.gkey[(u64)w * sc.cap_in + pm];
             T.key[(u64)w * T.cap + m] = k[w];
         }
-        T.re[m] = in.re[i];
-        T.im[m] = in.im[i];
+        T.re[m] = sc.gcoef[pm];
+        T.im[m] = sc.gcoef[sc.cap_in + pm];
         T.st[m] = 1;
         T.since[m] = 0;
         __threadfence_block();
@@ -360,15 +360,17 @@ __global__ void __launch_bounds__(kBlock) morbit_single(StoreView in, StoreView 
         }
         bool simple = na == 1 && m0 <= 2;
         u64 q0[KW], q1[KW];
-        u32 i0 = 0, i1 = 0;
+        u64 i0 = 0, i1 = 0;  // positions in group order (sc.gkey / sc.gcoef)
         const MBatchGate& G = a.gates[t < 0 ? 0 : t];
         if (simple) {
             const u32 base = sc.off[rep];
-            i0 = sc.order[base];
-            load_key<KW>(in, i0, q0);
+            i0 = base;
+#pragma unroll
+            for (int w = 0; w < KW; w++) q0[w] = sc.gkey[(u64)w * sc.cap_in + i0];
             if (m0 == 2) {
-                i1 = sc.order[base + 1];
-                load_key<KW>(in, i1, q1);
+                i1 = (u64)base + 1;
+#pragma unroll
+                for (int w = 0; w < KW; w++) q1[w] = sc.gkey[(u64)w * sc.cap_in + i1];
 #pragma unroll
                 for (int w = 0; w < KW; w++) simple = simple && (q1[w] == (q0[w] ^ G.p[w]));
             }
@@ -391,11 +393,11 @@ __global__ void __launch_bounds__(kBlock) morbit_single(StoreView in, StoreView 
         const cplx sQ = {(mQ & 1) ? -1.0 : 1.0, 0.0};
         const cplx sK = {(mK & 1) ? -1.0 : 1.0, 0.0};
         const cplx F = {G.fr, G.fi};
-        const cplx cq = load_coef<true>(in, i0);
+        const cplx cq = {sc.gcoef[i0], sc.gcoef[sc.cap_in + i0]};
         cplx nq, nk;
         bool has_k;
         if (m0 == 2) {
-            const cplx ck = load_coef<true>(in, i1);
+            const cplx ck = {sc.gcoef[i1], sc.gcoef[sc.cap_in + i1]};
             nq = cscale(cq, G.c);
             nk = cscale(ck, G.c);
             if (dQ <= a.maxdeg) nq = cadd(nq, cmul(cmul(ck, F), sK));

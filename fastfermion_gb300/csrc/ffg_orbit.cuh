@@ -52,6 +52,8 @@ struct OrbitScratch {
     u32* order;    // [cap_in] input positions grouped
     u32* groups;   // [cap_in] list of representatives
     u32* big;      // [cap_in] representatives of groups too large for a warp table
+    double* gcoef; // [2][cap_in] coefficients in group order (re, then im); after the
+                   // scatter gkey holds the keys in group order too
     u64* gslots;   // [2*cap_in] group index: (fingerprint << 32) | representative
     u64 gmask;
     u64 cap_in;
@@ -378,7 +380,12 @@ __global__ void __launch_bounds__(kBlock) orbit_offsets(OrbitScratch sc, OrbitCo
     }
 }
 
-__global__ void __launch_bounds__(kBlock) orbit_scatter(OrbitScratch sc, const OrbitCounters* oc) {
+// Members made contiguous: position p of a group's range gets the input
+// position (order) and a copy of the key planes (into gkey, no longer needed
+// for grouping) and of the coefficient, so that group processing reads one
+// contiguous range instead of gathering from the store.
+template <int KW, bool CPLX>
+__global__ void __launch_bounds__(kBlock) orbit_scatter(StoreView in, OrbitScratch sc, const OrbitCounters* oc) {
     wait_prior_grid();
     if (*(volatile const u32*)&oc->skip) return;
     const u64 n_in = *(volatile const u64*)&oc->n_in;
@@ -388,6 +395,10 @@ __global__ void __launch_bounds__(kBlock) orbit_scatter(OrbitScratch sc, const O
         if (r == 0xffffffffu) continue;
         const u32 p = sc.off[r] + atomicAdd(&sc.fill[r], 1u);
         sc.order[p] = (u32)i;
+#pragma unroll
+        for (int w = 0; w < KW; w++) sc.gkey[(u64)w * sc.cap_in + p] = in.key[(u64)w * in.cap + i];
+        sc.gcoef[p] = in.re[i];
+        if (CPLX) sc.gcoef[sc.cap_in + p] = in.im[i];
     }
 }
 
@@ -478,12 +489,11 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
         __syncwarp();
         for (u32 m = lane; m < m0; m += 32) {
             OCHK((u64)base + m < sc.cap_in, 11, base, m, rep)
-            const u32 i = sc.order[base + m];
-            OCHK(i < in.cap, 12, i, m, rep)
+            const u64 pm = (u64)base + m;
 #pragma unroll
-            for (int w = 0; w < KW; w++) T.key[m][w] = in.key[(u64)w * in.cap + i];
-            T.re[m] = in.re[i];
-            if (CPLX) T.im[m] = in.im[i];
+            for (int w = 0; w < KW; w++) T.key[m][w] = sc.gkey[(u64)w * sc.cap_in + pm];
+            T.re[m] = sc.gcoef[pm];
+            if (CPLX) T.im[m] = sc.gcoef[sc.cap_in + pm];
             table_insert<KW, CPLX>(T, T.key[m], (unsigned short)m);
         }
         if (lane == 0) {
@@ -743,17 +753,16 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
         }
         for (u32 m = threadIdx.x; m < m0; m += blockDim.x) {
             OCHK((u64)base + m < sc.cap_in, 1, base, m, rep)
-            const u32 i = sc.order[base + m];
-            OCHK(i < in.cap, 2, i, m, rep)
             OCHK(m < rcap, 3, m, rcap, rep)
+            const u64 pm = (u64)base + m;
             u64 k[KW];
 #pragma unroll
             for (int w = 0; w < KW; w++) {
-                k[w] = in.key[(u64)w * in.cap + i];
+                k[w] = sc.gkey[(u64)w * sc.cap_in + pm];
                 G.key[(u64)w * rcap + m] = k[w];
             }
-            G.re[m] = in.re[i];
-            if (CPLX) G.im[m] = in.im[i];
+            G.re[m] = sc.gcoef[pm];
+            if (CPLX) G.im[m] = sc.gcoef[sc.cap_in + pm];
             __threadfence_block();
             big_insert<KW, CPLX>(G, rcap, k, m);
         }
