@@ -944,7 +944,7 @@ struct Engine {
         OrbitScratch sc{};
         u64 hc = pow2_at_least(std::max<u64>(2 * cap_in, 1024));
         size_t need = align256((size_t)kAW * cap_in * 8) + align256((size_t)KW * cap_in * 8) +
-                      8 * align256(cap_in * 4) + align256(2 * cap_in * 8) + align256(hc * 8) + 256;
+                      9 * align256(cap_in * 4) + align256(2 * cap_in * 8) + align256(hc * 8) + 256;
         if (ctx->oscratch_bytes < need) {
             if (ctx->d_oscratch && cudaFree(ctx->d_oscratch) != cudaSuccess) return sc;
             ctx->d_oscratch = nullptr;
@@ -977,6 +977,8 @@ struct Engine {
         p += 256;
         sc.gcoef = (double*)p;
         p += align256(2 * cap_in * 8);
+        sc.list2 = (u32*)p;
+        p += align256(cap_in * 4);
         sc.gslots = (u64*)p;
         sc.gmask = hc - 1;
         sc.cap_in = cap_in;
@@ -1207,9 +1209,13 @@ struct Engine {
         a.route_big = ctx->orbit_route_big;
         const size_t wsm = (size_t)kMWarps * mtable_bytes<KW>(kMWarpCap);
         const size_t tsm = mtable_bytes<KW>(kMTeamCap);
+        const size_t ssm = (size_t)(32 * kMSubWarps / kMSubLanes) * mtable_bytes<KW>(kMSubCap);
         static bool attr_set = false;
-        static int team_per_sm = 1;
+        static int team_per_sm = 1, sub_per_sm = 1;
         if (!attr_set) {
+            CK(cudaFuncSetAttribute(morbit_sub<KW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sub_per_sm, morbit_sub<KW>, 32 * kMSubWarps, ssm));
+            sub_per_sm = std::max(sub_per_sm, 1);
             CK(cudaFuncSetAttribute(morbit_warp<KW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
             CK(cudaFuncSetAttribute(morbit_block<KW, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)tsm));
@@ -1235,12 +1241,15 @@ struct Engine {
                 OSTEP("orbit_scatter");
                 morbit_single<KW><<<G, kBlock, 0, ctx->stream>>>(cur.v, dst.v, sc, oc, a);
                 OSTEP("morbit_single");
+                morbit_sub<KW><<<ctx->num_sms * sub_per_sm, 32 * kMSubWarps, ssm, ctx->stream>>>(cur.v, dst.v, sc,
+                                                                                              oc, a);
+                OSTEP("morbit_sub");
                 morbit_warp<KW><<<ctx->num_sms * 2, 32 * kMWarps, wsm, ctx->stream>>>(cur.v, dst.v, sc, oc, a);
                 OSTEP("morbit_warp");
                 morbit_block<KW, 256, true><<<ctx->num_sms * team_per_sm, 256, tsm, ctx->stream>>>(
                     cur.v, dst.v, sc, oc, a, kMTeamCap, nullptr, 0, sc.big, 0, &oc->nbig, retry_list, nretry);
                 OSTEP("morbit_block");
-                ctx->prof.kernel_launches += 8;
+                ctx->prof.kernel_launches += 9;
             }
             u32 nleft = 0;
             CK(cudaMemcpyAsync(ctx->h_oc, oc, sizeof(OrbitCounters), cudaMemcpyDeviceToHost, ctx->stream));

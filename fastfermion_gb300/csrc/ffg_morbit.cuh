@@ -432,6 +432,45 @@ __global__ void __launch_bounds__(kBlock) morbit_single(StoreView in, StoreView 
     if (threadIdx.x == 0 && tot) atomicAdd(&oc->emits, (u64)tot);
 }
 
+constexpr u32 kMSubCap = 64;      // sub-warp tier: members per group table
+constexpr int kMSubLanes = 8;     // sub-warp tier: lanes per group (4 groups per warp)
+constexpr int kMSubWarps = 8;     // sub-warp tier: warps per block
+
+// Sub-warp tier: 8 lanes per group, 64-member tables in shared memory, for the
+// groups whose orbit bound m0 * 2^|A| is at most 64 (they cannot outgrow the
+// table); the others go to sc.list2 for the warp tier.
+template <int KW>
+__global__ void __launch_bounds__(32 * kMSubWarps) morbit_sub(StoreView in, StoreView out, OrbitScratch sc,
+                                                            OrbitCounters* oc, MOrbitArgs a) {
+    extern __shared__ __align__(16) unsigned char msm[];
+    if (*(volatile u32*)&oc->skip) return;
+    constexpr int kTeams = 32 * kMSubWarps / kMSubLanes;
+    const int team = threadIdx.x / kMSubLanes, rank = threadIdx.x % kMSubLanes;
+    const MTable<KW> T = mcarve<KW>((char*)msm + team * mtable_bytes<KW>(kMSubCap), kMSubCap);
+    const u32 ng = *(volatile u32*)&oc->nrest;  // groups left by morbit_single, listed in sc.fill
+    long long apps = 0, emits = 0;
+    for (u32 g = blockIdx.x * kTeams + team; g < ng; g += gridDim.x * kTeams) {
+        const u32 rep = sc.fill[g];
+        int na = 0;
+#pragma unroll
+        for (int w = 0; w < kAW; w++) na += __popcll(sc.amask[(u64)w * sc.cap_in + rep]);
+        const u32 m0 = sc.cnt[rep];
+        bool done = false;
+        if (na < 7 && ((u64)m0 << na) <= kMSubCap)
+            done = mgroup<KW, kMSubLanes>(in, out, sc, oc, a, T, rep, rank, apps, emits);
+        if (!done && rank == 0) sc.list2[atomicAdd(&oc->nrest2, 1u)] = rep;
+        team_sync<kMSubLanes>();
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        apps += __shfl_down_sync(0xffffffffu, apps, o);
+        emits += __shfl_down_sync(0xffffffffu, emits, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (apps) atomicAdd(&oc->xapps, (u64)apps);
+        if (emits) atomicAdd(&oc->emits, (u64)emits);
+    }
+}
+
 constexpr u32 kMWarpCap = 256;    // warp tier: members per group table
 constexpr int kMWarps = 8;        // warp tier: groups per block
 constexpr u32 kMTeamCap = 1024;   // team tier (256 threads)
@@ -445,10 +484,10 @@ __global__ void __launch_bounds__(32 * kMWarps) morbit_warp(StoreView in, StoreV
     if (*(volatile u32*)&oc->skip) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const MTable<KW> T = mcarve<KW>((char*)msm + warp * mtable_bytes<KW>(kMWarpCap), kMWarpCap);
-    const u32 ng = *(volatile u32*)&oc->nrest;  // groups left by morbit_single, listed in sc.fill
+    const u32 ng = *(volatile u32*)&oc->nrest2;  // groups left by morbit_sub, listed in sc.list2
     long long apps = 0, emits = 0;
     for (u32 g = blockIdx.x * kMWarps + warp; g < ng; g += gridDim.x * kMWarps) {
-        const u32 rep = sc.fill[g];
+        const u32 rep = sc.list2[g];
         int na = 0;
 #pragma unroll
         for (int w = 0; w < kAW; w++) na += __popcll(sc.amask[(u64)w * sc.cap_in + rep]);

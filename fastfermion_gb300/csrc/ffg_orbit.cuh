@@ -52,6 +52,7 @@ struct OrbitScratch {
     u32* order;    // [cap_in] input positions grouped
     u32* groups;   // [cap_in] list of representatives
     u32* big;      // [cap_in] representatives of groups too large for a warp table
+    u32* list2;    // [cap_in] groups passed on by the Majorana sub-warp tier
     double* gcoef; // [2][cap_in] coefficients in group order (re, then im); after the
                    // scatter gkey holds the keys in group order too
     u64* gslots;   // [2*cap_in] group index: (fingerprint << 32) | representative
@@ -78,6 +79,7 @@ struct OrbitCounters {
     u32 skip;          // 1: an earlier batch of the window did not complete; this one does nothing
     u32 member_total;  // members placed by orbit_offsets
     u32 nrest;         // groups left by a thread-level pass for the warp tier (list in OrbitScratch::fill)
+    u32 nrest2;        // groups left by a sub-warp pass (list in OrbitScratch::list2)
     u64 n_in;          // terms entering the batch (set by orbit_gate)
     u64 gmask;         // group-index slots - 1 for this batch (set by orbit_gate)
 };
@@ -126,10 +128,15 @@ __device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol
 // barrier of a team of TEAM threads (a warp, or the whole block)
 template <int TEAM>
 __device__ __forceinline__ void team_sync() {
-    if (TEAM == 32)
+    if (TEAM < 32) {
+        // the TEAM-lane slice of the warp that this thread belongs to
+        const unsigned lane = threadIdx.x & 31;
+        __syncwarp(((1u << TEAM) - 1) << (lane & ~(unsigned)(TEAM - 1)));
+    } else if (TEAM == 32) {
         __syncwarp();
-    else
+    } else {
         __syncthreads();
+    }
 }
 
 // instance of the group represented by input position rep
