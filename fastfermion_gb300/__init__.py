@@ -6,6 +6,7 @@ gate types (H, S, CNOT, SWAP, CZ, ROT, MROT), polynomial types and product
 states, backed by hand-written CUDA kernels in libffg (C ABI: include/ffg.h).
 """
 from . import workloads
+from .autotune import autotune
 from .majorana import FockState, MajoranaPolynomial, MajoranaString, MROT, jw, majoranas
 from .parse import poly
 from .pauli import CNOT, CZ, H, MAX_QUBITS, ROT, S, SWAP, PauliPolynomial, PauliString, QubitProductState, paulis
@@ -32,4 +33,4 @@ __all__ = ["PauliString", "PauliPolynomial", "MajoranaString", "MajoranaPolynomi
            "CNOT", "SWAP", "CZ", "ROT", "MROT", "QubitProductState", "FockState", "propagate",
            "poly", "paulis", "majoranas", "profile_reset", "profile_disable", "profile_get",
            "last_profile", "has_openmp", "MAX_QUBITS", "build_circuit", "workloads",
-           "encode_pauli_circuit", "encode_majorana_circuit", "jw"]
+           "encode_pauli_circuit", "encode_majorana_circuit", "jw", "autotune"]

@@ -57,7 +57,8 @@ EXPORTS = ["ffg_create", "ffg_destroy", "ffg_last_error", "ffg_set_profiling", "
            "ffg_result_qubit_state", "ffg_result_fock_state", "ffg_result_free", "ffg_abs_le",
            "ffg_pauli_schedule", "ffg_stream", "ffg_pauli_rotations_noalloc",
            "ffg_pauli_propagate_batched", "ffg_batch_size", "ffg_batch_copy", "ffg_batch_adjoint",
-           "ffg_batch_free", "ffg_majorana_to_pauli", "ffg_result_sparse"]
+           "ffg_batch_free", "ffg_majorana_to_pauli", "ffg_result_sparse", "ffg_set_option",
+           "ffg_get_option"]
 
 
 def lib():
@@ -106,6 +107,8 @@ def lib():
             L.ffg_batch_free.argtypes = [vp]
             L.ffg_majorana_to_pauli.argtypes = [vp, vp, vp, vp, sz, ctypes.c_int, ctypes.POINTER(vp)]
             L.ffg_result_sparse.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, sz, ctypes.POINTER(sz)]
+            L.ffg_set_option.argtypes = [vp, ctypes.c_char_p, i64]
+            L.ffg_get_option.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(i64)]
             L.ffg_pauli_schedule.restype = i64
             L.ffg_pauli_schedule.argtypes = [vp, sz, ctypes.c_int, vp, i64]
             _lib = L
@@ -139,6 +142,17 @@ class Context:
             if rc == -1:
                 raise RuntimeError(msg)
             raise FFGError(f"libffg error {rc}: {msg}")
+
+    OPTIONS = ("orbit_route_big", "orbit_team", "orbit_window", "orbit_min_gates", "orbit_qidx", "pdl",
+               "morbit", "morbit_min_gates")
+
+    def set_option(self, name, value):
+        self.check(self.L.ffg_set_option(self.h, name.encode(), int(value)))
+
+    def get_option(self, name):
+        v = ctypes.c_int64()
+        self.check(self.L.ffg_get_option(self.h, name.encode(), ctypes.byref(v)))
+        return int(v.value)
 
     def stream(self):
         """cudaStream_t of the context (integer handle)."""

@@ -117,6 +117,8 @@ struct PendingEvent {
     int phase;
 };
 
+constexpr int kOrbitWindowMax = 16;  // orbit batches enqueued per host round trip (at most)
+
 // One step of a batched propagation, kept for the adjoint: a range of Clifford
 // ops run by the persistent kernel, or one orbit batch.
 struct AdjRecord {
@@ -178,6 +180,7 @@ struct ffg_ctx {
     bool morbit = true;         // batch-orbit path for commuting Majorana runs (FFG_MORBIT=0 disables)
     bool pdl = true;            // programmatic dependent launch of the orbit kernels (FFG_PDL=0 disables)
     bool orbit_qidx = true;     // classify against the gates on each term's support (FFG_ORBIT_QIDX=0 disables)
+    int orbit_window = kOrbitWindowMax;  // orbit batches per host round trip (1..kOrbitWindowMax)
     int morbit_min_gates = 2;   // shortest Majorana run sent to the batch-orbit path
     MBatchGate* d_mgates = nullptr;
     size_t mgates_cap = 0;
@@ -189,7 +192,7 @@ struct ffg_ctx {
     size_t oscratch_bytes = 0;
     OrbitCounters* d_oc = nullptr;
     OrbitCounters* h_oc = nullptr;  // pinned
-    OrbitCounters* d_ocw = nullptr;  // counters of a window of orbit batches (kOrbitWindow)
+    OrbitCounters* d_ocw = nullptr;  // counters of a window of orbit batches (kOrbitWindowMax)
     OrbitCounters* h_ocw = nullptr;  // pinned
     RawBuf bigpool;                 // global-memory tables of large orbit groups
     const BatchCtx* batch = nullptr;  // set while a batched propagation runs
@@ -239,7 +242,6 @@ struct ffg_batch {
 namespace {
 
 constexpr int kMaxParts = 1024;
-constexpr int kOrbitWindow = 16;  // orbit batches enqueued per host round trip
 constexpr int kChunkOps = 128;
 
 #define CK(call)                                                                          \
@@ -1012,7 +1014,7 @@ struct Engine {
     }
 
     // Runs consecutive orbit batches on the (dense) live store.  Up to
-    // kOrbitWindow batches are enqueued back to back, ping-ponging between the
+    // orbit_window batches are enqueued back to back, ping-ponging between the
     // two store buffers sized for the window, with no host round trip: every
     // kernel reads its input size from the batch's counters (orbit_gate).  The
     // host then reads all counters once and walks the batches: completed ones
@@ -1062,7 +1064,7 @@ struct Engine {
             Store S[2] = {cur, carve(ctx->buf[1 - active], KW, CPLX, wcap)};
             OrbitScratch sc = carve_scratch(wcap);
             if (!sc.amask) return set_err(ctx, FFG_ERR_CUDA, "orbit scratch allocation failed");
-            const int m = std::min(kOrbitWindow, njobs - i);
+            const int m = std::min(std::max(1, std::min(ctx->orbit_window, kOrbitWindowMax)), njobs - i);
             {
                 PhaseScope ps(ctx, PH_ROT);
                 for (int j = 0; j < m; j++) {
@@ -1232,22 +1234,26 @@ struct Engine {
             OrbitCounters* oc = ctx->d_oc;
             {
                 PhaseScope ps(ctx, PH_ROT);
-                orbit_gate<<<1, 32, 0, ctx->stream>>>(oc, nullptr, n_in, sc.gmask + 1, nretry);
-                morbit_classify<KW><<<G, kBlock, 0, ctx->stream>>>(cur.v, dst.v, sc, oc, a);
+                const bool pdl = ctx->pdl;
+                const StoreView in = cur.v, ov = dst.v;
+                CK(launch_k(pdl, orbit_gate, 1, 32, 0, ctx->stream, oc, (const OrbitCounters*)nullptr, n_in,
+                            sc.gmask + 1, nretry));
+                CK(launch_k(pdl, morbit_classify<KW>, G, kBlock, 0, ctx->stream, in, ov, sc, oc, a));
                 OSTEP("morbit_classify");
-                orbit_group<KW><<<G, kBlock, 0, ctx->stream>>>(sc, oc);
-                orbit_offsets<<<G, kBlock, 0, ctx->stream>>>(sc, oc);
-                orbit_scatter<KW, true><<<G, kBlock, 0, ctx->stream>>>(cur.v, sc, oc);
+                CK(launch_k(pdl, orbit_group<KW>, G, kBlock, 0, ctx->stream, sc, oc));
+                CK(launch_k(pdl, orbit_offsets, G, kBlock, 0, ctx->stream, sc, oc));
+                CK(launch_k(pdl, orbit_scatter<KW, true>, G, kBlock, 0, ctx->stream, in, sc, (const OrbitCounters*)oc));
                 OSTEP("orbit_scatter");
-                morbit_single<KW><<<G, kBlock, 0, ctx->stream>>>(cur.v, dst.v, sc, oc, a);
+                CK(launch_k(pdl, morbit_single<KW>, G, kBlock, 0, ctx->stream, in, ov, sc, oc, a));
                 OSTEP("morbit_single");
-                morbit_sub<KW><<<ctx->num_sms * sub_per_sm, 32 * kMSubWarps, ssm, ctx->stream>>>(cur.v, dst.v, sc,
-                                                                                              oc, a);
+                CK(launch_k(pdl, morbit_sub<KW>, ctx->num_sms * sub_per_sm, 32 * kMSubWarps, ssm, ctx->stream, in, ov,
+                            sc, oc, a));
                 OSTEP("morbit_sub");
-                morbit_warp<KW><<<ctx->num_sms * 2, 32 * kMWarps, wsm, ctx->stream>>>(cur.v, dst.v, sc, oc, a);
+                CK(launch_k(pdl, morbit_warp<KW>, ctx->num_sms * 2, 32 * kMWarps, wsm, ctx->stream, in, ov, sc, oc, a));
                 OSTEP("morbit_warp");
-                morbit_block<KW, 256, true><<<ctx->num_sms * team_per_sm, 256, tsm, ctx->stream>>>(
-                    cur.v, dst.v, sc, oc, a, kMTeamCap, nullptr, 0, sc.big, 0, &oc->nbig, retry_list, nretry);
+                CK(launch_k(pdl, morbit_block<KW, 256, true>, ctx->num_sms * team_per_sm, 256, tsm, ctx->stream, in, ov,
+                            sc, oc, a, (u32)kMTeamCap, (char*)nullptr, (u64)0, (const u32*)sc.big, 0u,
+                            (const u32*)&oc->nbig, retry_list, nretry));
                 OSTEP("morbit_block");
                 ctx->prof.kernel_launches += 9;
             }
@@ -2169,8 +2175,8 @@ int ffg_create(ffg_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ps, sizeof(PersistState));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_oc, sizeof(OrbitCounters));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_oc, sizeof(OrbitCounters));
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ocw, kOrbitWindow * sizeof(OrbitCounters));
-    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_ocw, kOrbitWindow * sizeof(OrbitCounters));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ocw, kOrbitWindowMax * sizeof(OrbitCounters));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_ocw, kOrbitWindowMax * sizeof(OrbitCounters));
     if (e != cudaSuccess) {
         fprintf(stderr, "ffg_create: %s\n", cudaGetErrorString(e));
         ffg_destroy(ctx);
@@ -3056,4 +3062,50 @@ int ffg_result_sparse(const ffg_result* r, int n, int64_t* indptr, int64_t* indi
     } catch (const std::exception& ex) {
         return set_err(ctx, FFG_ERR_STATE, ex.what());
     }
+}
+
+// ---------------------------------------------------------------------------
+// engine options (the tuning knobs; defaults as measured on GB300)
+// ---------------------------------------------------------------------------
+namespace {
+struct OptionRef {
+    const char* name;
+    int (*get)(const ffg_ctx*);
+    bool (*set)(ffg_ctx*, int64_t);
+};
+const OptionRef kOptions[] = {
+    {"orbit_route_big", [](const ffg_ctx* c) { return c->orbit_route_big; },
+     [](ffg_ctx* c, int64_t v) { if (v < 1 || v > 1 << 20) return false; c->orbit_route_big = (int)v; return true; }},
+    {"orbit_team", [](const ffg_ctx* c) { return (int)c->orbit_team; },
+     [](ffg_ctx* c, int64_t v) { c->orbit_team = v != 0; return true; }},
+    {"orbit_window", [](const ffg_ctx* c) { return c->orbit_window; },
+     [](ffg_ctx* c, int64_t v) { if (v < 1 || v > kOrbitWindowMax) return false; c->orbit_window = (int)v; return true; }},
+    {"orbit_min_gates", [](const ffg_ctx* c) { return c->orbit_min_gates; },
+     [](ffg_ctx* c, int64_t v) { if (v < 1) return false; c->orbit_min_gates = (int)v; return true; }},
+    {"orbit_qidx", [](const ffg_ctx* c) { return (int)c->orbit_qidx; },
+     [](ffg_ctx* c, int64_t v) { c->orbit_qidx = v != 0; return true; }},
+    {"pdl", [](const ffg_ctx* c) { return (int)c->pdl; }, [](ffg_ctx* c, int64_t v) { c->pdl = v != 0; return true; }},
+    {"morbit", [](const ffg_ctx* c) { return (int)c->morbit; },
+     [](ffg_ctx* c, int64_t v) { c->morbit = v != 0; return true; }},
+    {"morbit_min_gates", [](const ffg_ctx* c) { return c->morbit_min_gates; },
+     [](ffg_ctx* c, int64_t v) { if (v < 1) return false; c->morbit_min_gates = (int)v; return true; }},
+};
+}  // namespace
+
+int ffg_set_option(ffg_ctx* ctx, const char* name, int64_t value) {
+    if (!ctx || !name) return FFG_ERR_ARG;
+    for (const OptionRef& o : kOptions)
+        if (std::strcmp(o.name, name) == 0)
+            return o.set(ctx, value) ? FFG_OK : set_err(ctx, FFG_ERR_ARG, std::string("bad value for ") + name);
+    return set_err(ctx, FFG_ERR_ARG, std::string("unknown option ") + name);
+}
+
+int ffg_get_option(const ffg_ctx* ctx, const char* name, int64_t* value) {
+    if (!ctx || !name || !value) return FFG_ERR_ARG;
+    for (const OptionRef& o : kOptions)
+        if (std::strcmp(o.name, name) == 0) {
+            *value = o.get(ctx);
+            return FFG_OK;
+        }
+    return FFG_ERR_ARG;
 }

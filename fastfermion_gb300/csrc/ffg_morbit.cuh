@@ -57,6 +57,7 @@ __device__ __forceinline__ bool manti(const u64* q, const u64* p, int odd) {
 template <int KW>
 __global__ void __launch_bounds__(kBlock) morbit_classify(StoreView in, StoreView out, OrbitScratch sc,
                                                           OrbitCounters* oc, MOrbitArgs a) {
+    wait_prior_grid();
     if (*(volatile u32*)&oc->skip) return;
     const u64 n_in = *(volatile u64*)&oc->n_in;
     const u64 nslots = *(volatile u64*)&oc->gmask + 1;
@@ -343,6 +344,7 @@ __device__ bool mgroup(const StoreView& in, const StoreView& out, const OrbitScr
 template <int KW>
 __global__ void __launch_bounds__(kBlock) morbit_single(StoreView in, StoreView out, OrbitScratch sc,
                                                         OrbitCounters* oc, MOrbitArgs a) {
+    wait_prior_grid();
     if (*(volatile u32*)&oc->skip) return;
     const u32 ng = *(volatile u32*)&oc->ngroups;
     __shared__ long long sh[kBlock / 32];
@@ -442,6 +444,7 @@ constexpr int kMSubWarps = 8;     // sub-warp tier: warps per block
 template <int KW>
 __global__ void __launch_bounds__(32 * kMSubWarps) morbit_sub(StoreView in, StoreView out, OrbitScratch sc,
                                                             OrbitCounters* oc, MOrbitArgs a) {
+    wait_prior_grid();
     extern __shared__ __align__(16) unsigned char msm[];
     if (*(volatile u32*)&oc->skip) return;
     constexpr int kTeams = 32 * kMSubWarps / kMSubLanes;
@@ -480,6 +483,7 @@ constexpr u32 kMTeamCap = 1024;   // team tier (256 threads)
 template <int KW>
 __global__ void __launch_bounds__(32 * kMWarps) morbit_warp(StoreView in, StoreView out, OrbitScratch sc,
                                                           OrbitCounters* oc, MOrbitArgs a) {
+    wait_prior_grid();
     extern __shared__ __align__(16) unsigned char msm[];
     if (*(volatile u32*)&oc->skip) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -516,6 +520,7 @@ __global__ void __launch_bounds__(TB) morbit_block(StoreView in, StoreView out, 
                                                    MOrbitArgs a, u32 cap, char* pool, u64 region_bytes,
                                                    const u32* list, u32 nlist, const u32* nlist_dev, u32* retry,
                                                    u32* nretry) {
+    wait_prior_grid();
     extern __shared__ __align__(16) unsigned char msm[];
     if (*(volatile u32*)&oc->skip) return;
     if (nlist_dev) nlist = *(volatile const u32*)nlist_dev;

@@ -129,6 +129,20 @@ int ffg_profile_get(const ffg_ctx* ctx, ffg_profile* out);
  * work around the library's launches. */
 void* ffg_stream(const ffg_ctx* ctx);
 
+/* Engine options (no counterpart in the reference): runtime knobs of the
+ * orbit engine, tuned by fastfermion_gb300.autotune.  Names:
+ *   orbit_route_big   |A| from which a Pauli group skips the warp tier (default 8)
+ *   orbit_team        1: 256-thread team tier before the 1024-thread tier (1)
+ *   orbit_window      orbit batches per host round trip, 1..16 (16)
+ *   orbit_min_gates   shortest commuting run sent to the orbit path (4)
+ *   orbit_qidx        1: classify against the gates on each term's support (1)
+ *   pdl               1: programmatic dependent launch of the orbit kernels (1)
+ *   morbit            1: orbit path for commuting Majorana runs (1)
+ *   morbit_min_gates  shortest Majorana run sent to the orbit path (2)
+ * Results do not depend on the options (only speed does). */
+int ffg_set_option(ffg_ctx* ctx, const char* name, int64_t value);
+int ffg_get_option(const ffg_ctx* ctx, const char* name, int64_t* value);
+
 /* Truncated Heisenberg propagation of a Pauli polynomial through a circuit.
  * keys/re/im are host pointers when on_device == 0, device pointers of the
  * context's device otherwise.  The result stays on the device until copied. */

@@ -107,3 +107,26 @@ def test_reference_quirk_unknown_strategy_returns_input():
     obs = ff.PauliString("Z0")
     r = ff.propagate([ff.ROT("X", [0], 0.3)], obs, n_threads=4, parallel="bogus")
     assert len(r) == 1
+
+
+@pytest.mark.gpu
+def test_engine_options_and_autotune():
+    """Options change speed only; the tuner checks that and keeps the fastest."""
+    from fastfermion_gb300 import _native
+    ctx = _native.context(0)
+    before = {k: ctx.get_option(k) for k in ctx.OPTIONS}
+    with pytest.raises(RuntimeError):
+        ctx.set_option("orbit_window", 99)
+    with pytest.raises(RuntimeError):
+        ctx.set_option("no_such_option", 1)
+    circ = ff.build_circuit(ff.workloads.kicked_ising_circuit(0.5, 6, 6, 8))
+    obs = ff.PauliString([(21, "Z")])
+    ref = ff.propagate(circ, obs, maxdegree=6, mincoeff=1e-5)
+    res = ff.autotune(circ, obs, repeats=1, maxdegree=6, mincoeff=1e-5)
+    from fastfermion_gb300.autotune import DEFAULT_SPACE
+    assert set(res["options"]) == set(DEFAULT_SPACE)
+    assert len(res["timings"]) >= 5
+    tuned = ff.propagate(circ, obs, maxdegree=6, mincoeff=1e-5)
+    assert len(tuned) == len(ref) and tuned.overlapwithzero() == pytest.approx(ref.overlapwithzero(), abs=1e-12)
+    for k, v in before.items():
+        ctx.set_option(k, v)
