@@ -6,7 +6,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libffg.so")
-SOURCES = ["ffg_engine.cu", "ffg_noalloc.cu"]
+SOURCES = ["ffg_engine.cu", "ffg_noalloc.cu", "ffg_sortmerge.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -27,17 +27,26 @@ def _stale():
 
 
 def build(force=False, verbose=False):
-    """Compile libffg.so unless it is up to date; returns its path."""
+    """Compile libffg.so unless it is up to date (translation units in
+    parallel, then one link); returns its path."""
     if not force and not _stale():
         return LIB
     extra = os.environ.get("FFG_BUILD_FLAGS", "").split()
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", *extra,
-           "-Xcompiler", "-fPIC,-ffp-contract=off", "-shared",
-           "-I", os.path.join(os.path.dirname(HERE), "include"),
-           *[os.path.join(CSRC, s) for s in SOURCES], "-o", LIB + ".tmp"]
+    common = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", *extra,
+              "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", os.path.join(os.path.dirname(HERE), "include")]
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    subprocess.run(cmd, check=True)
+        common.insert(1, "-Xptxas=-v")
+    objs, procs = [], []
+    for src in SOURCES:
+        obj = os.path.join(CSRC, src[:-3] + ".o")
+        objs.append(obj)
+        procs.append(subprocess.Popen([*common, "-c", os.path.join(CSRC, src), "-o", obj]))
+    codes = [p.wait() for p in procs]
+    if any(codes):
+        raise subprocess.CalledProcessError(next(c for c in codes if c), "nvcc")
+    subprocess.run([nvcc(), *ARCH, "-shared", *objs, "-o", LIB + ".tmp"], check=True)
+    for o in objs:
+        os.remove(o)
     os.replace(LIB + ".tmp", LIB)
     return LIB
 

@@ -35,6 +35,7 @@
 #include "ffg_adjoint.cuh"
 #include "ffg_morbit.cuh"
 #include "ffg_transforms.cuh"
+#include "ffg_sortmerge.h"
 
 using namespace ffg;
 
@@ -181,6 +182,9 @@ struct ffg_ctx {
     bool pdl = true;            // programmatic dependent launch of the orbit kernels (FFG_PDL=0 disables)
     bool orbit_qidx = true;     // classify against the gates on each term's support (FFG_ORBIT_QIDX=0 disables)
     int orbit_window = kOrbitWindowMax;  // orbit batches per host round trip (1..kOrbitWindowMax)
+    bool merge_sort = false;    // per-gate sort-and-reduce merge instead of the hash / orbit paths
+    void* d_smscratch = nullptr;
+    size_t smscratch_bytes = 0;
     int morbit_min_gates = 2;   // shortest Majorana run sent to the batch-orbit path
     MBatchGate* d_mgates = nullptr;
     size_t mgates_cap = 0;
@@ -1174,6 +1178,83 @@ struct Engine {
     }
 
     // ---------------------------------------------------------------------
+    // per-gate sort-and-reduce merge (option merge_sort; Pauli)
+    // ---------------------------------------------------------------------
+    int run_sortmerge(const std::vector<Op>& ops, const std::vector<TruncArgs>& truncs,
+                      const std::vector<GArgs>& groups) {
+        index_valid = false;
+        for (size_t i = 0; i < ops.size(); i++) {
+            const Op& o = ops[i];
+            if (o.type == Op::GROUP) {
+                const GArgs& ga = groups[o.idx];
+                if (ga.ng != 1) return set_err(ctx, FFG_ERR_ARG, "merge_sort needs one rotation per pass");
+                ffg_sm::SmGate g{};
+                for (int w = 0; w < 4; w++) g.p[w] = ga.psub[1][w];
+                g.c = ga.c[0];
+                g.s = ga.s[0];
+                g.yP = ga.yP[0];
+                g.maxdeg = ga.maxdeg;
+                const u64 n_in = ctx->h_ctr->n;
+                u64 out_cap = std::max<u64>(cap, pow2_at_least(2 * n_in));
+                for (int attempt = 0; attempt < 4; attempt++) {
+                    int rc = ensure_buf(ctx, ctx->buf[1 - active], store_bytes(KW, CPLX, out_cap));
+                    if (rc) return rc;
+                    Store dst = carve(ctx->buf[1 - active], KW, CPLX, out_cap);
+                    u64 n_out = 0, em = 0;
+                    int e;
+                    {
+                        PhaseScope ps(ctx, PH_ROT);
+                        e = ffg_sm::rotation(ctx->stream, KW, CPLX, cur.v.key, cur.v.re, CPLX ? cur.v.im : nullptr,
+                                             n_in, cap, g, dst.v.key, dst.v.re, CPLX ? dst.v.im : nullptr, out_cap,
+                                             &n_out, &em, &ctx->d_smscratch, &ctx->smscratch_bytes);
+                    }
+                    if (e) return set_err(ctx, FFG_ERR_CUDA, std::string("sort-merge pass: ") +
+                                                                 cudaGetErrorString((cudaError_t)e));
+                    ctx->prof.kernel_launches += 5;
+                    ctx->prof.syncs++;
+                    if (n_out > out_cap) {
+                        out_cap = pow2_at_least(n_out);
+                        continue;
+                    }
+                    CK(cudaMemsetAsync(dst.v.dead, 0, n_out, ctx->stream));
+                    cur = dst;
+                    cap = out_cap;
+                    active = 1 - active;
+                    DevCounters h = *ctx->h_ctr;
+                    h.apps += n_in;
+                    h.emits += em;
+                    h.n = h.alive = n_out;
+                    if (n_out > h.peak) h.peak = n_out;
+                    *ctx->h_ctr = h;
+                    CK(cudaMemcpyAsync(ctx->d_ctr, ctx->h_ctr, sizeof(DevCounters), cudaMemcpyHostToDevice,
+                                       ctx->stream));
+                    break;
+                }
+            } else if (o.type == Op::TRUNC) {
+                if (o.topk > 0) return set_err(ctx, FFG_ERR_ARG, "merge_sort does not support top-k truncation");
+                TruncArgs t = truncs[o.idx];
+                t.op = (u32)i;
+                if (t.thr || t.max_xweight >= 0) launch_trunc(t);
+                int rc = sync_counters();
+                if (rc) return rc;
+                if (ctx->h_ctr->n != ctx->h_ctr->alive) {
+                    rc = compact_into(1 - active, cap);
+                    if (rc) return rc;
+                    rc = sync_counters();
+                    if (rc) return rc;
+                }
+            } else if (o.type == Op::CLIFF) {
+                launch_cliff(o.begin, o.end, (u32)i);
+                int rc = sync_counters();
+                if (rc) return rc;
+            } else {
+                return set_err(ctx, FFG_ERR_ARG, "merge_sort: unexpected op");
+            }
+        }
+        return finish();
+    }
+
+    // ---------------------------------------------------------------------
     // Majorana runs (batch-orbit path with the threshold after every gate)
     // ---------------------------------------------------------------------
     int upload_mgates(const std::vector<RotArgs>& rots) {
@@ -1819,6 +1900,8 @@ int run_engine(ffg_ctx* ctx, const uint64_t* keys, const double* re, const doubl
     for (const Op& o : ops) has_topk = has_topk || (o.type == Op::TRUNC && o.topk > 0);
     if (!PAULI && mruns && ctx->morbit && ctx->persistent)
         rc = E.run_majorana(ops, rots, truncs, *mruns, maxdeg);
+    else if (PAULI && ctx->merge_sort && ctx->group_d == 1)
+        rc = E.run_sortmerge(ops, truncs, groups);
     else if (has_topk)
         rc = E.run(ops, rots, truncs, groups);
     else if (PAULI && binfo && ctx->orbit && ctx->persistent && ctx->group_d == 1)
@@ -2205,6 +2288,7 @@ int ffg_destroy(ffg_ctx* ctx) {
     if (ctx->d_bgates) cudaFree(ctx->d_bgates);
     if (ctx->d_mgates) cudaFree(ctx->d_mgates);
     if (ctx->d_qidx) cudaFree(ctx->d_qidx);
+    if (ctx->d_smscratch) cudaFree(ctx->d_smscratch);
     if (ctx->d_oscratch) cudaFree(ctx->d_oscratch);
     if (ctx->bigpool.p) cudaFree(ctx->bigpool.p);
     if (ctx->d_oc) cudaFree(ctx->d_oc);
@@ -3087,6 +3171,8 @@ const OptionRef kOptions[] = {
     {"pdl", [](const ffg_ctx* c) { return (int)c->pdl; }, [](ffg_ctx* c, int64_t v) { c->pdl = v != 0; return true; }},
     {"morbit", [](const ffg_ctx* c) { return (int)c->morbit; },
      [](ffg_ctx* c, int64_t v) { c->morbit = v != 0; return true; }},
+    {"merge_sort", [](const ffg_ctx* c) { return (int)c->merge_sort; },
+     [](ffg_ctx* c, int64_t v) { c->merge_sort = v != 0; return true; }},
     {"morbit_min_gates", [](const ffg_ctx* c) { return c->morbit_min_gates; },
      [](ffg_ctx* c, int64_t v) { if (v < 1) return false; c->morbit_min_gates = (int)v; return true; }},
 };

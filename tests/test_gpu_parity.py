@@ -78,3 +78,23 @@ def test_apps_counter_matches_oracle():
         run_gpu(fx)
         p = _native.context(0).profile()
         assert p["apps"] == run_oracle(fx).apps, name
+
+
+SORT_MERGE = [n for n in EXACT if str(load(n)["kind"]) == "pauli" and float(load(n)["ref_seconds"]) < 2.0]
+
+
+@pytest.mark.parametrize("name", SORT_MERGE)
+def test_sort_merge_path_matches_reference(name):
+    """The radix-sort + segmented-reduce merge (engine option merge_sort)
+    reproduces the reference's term sets bit for bit, like the hash paths."""
+    from fastfermion_gb300 import _native
+    ctx = _native.context(0)
+    ctx.set_option("merge_sort", 1)
+    try:
+        fx = load(name)
+        r = run_gpu(fx)
+        keys, re, im = r.copy()
+        assert r.n == int(fx["n_terms"])
+        assert checksum(keys, re, im) == str(fx["checksum"])
+    finally:
+        ctx.set_option("merge_sort", 0)
