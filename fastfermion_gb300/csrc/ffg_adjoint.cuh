@@ -33,7 +33,7 @@ namespace ffg {
 
 constexpr u32 kAdjWarpCap = 256;     // members of a group held in shared memory (warp tier)
 constexpr u32 kAdjWarpGates = 9;     // gates of a warp-tier group (history rows in shared memory)
-constexpr int kAdjWarps = 4;          // groups in flight per block (warp tier)
+constexpr int kAdjWarps = 3;          // groups in flight per block (warp tier; 3 keeps two blocks per SM)
 constexpr unsigned short kInputMember = 0xffff;
 
 // Tables of one group.  Warp tier: in shared memory; block tier: in the block's

@@ -2071,7 +2071,11 @@ int batch_adjoint(ffg_batch* h, const double* weights, double* grad_theta, doubl
     out.key = h->fkey;
     out.re = h->fre;
     out.cap = h->fn;
-    CK(cudaMalloc(&B.abar_out, std::max<u64>(h->fn, 1) * 8));
+    // abar buffers sized once for the largest term set of any step
+    u64 nmax = std::max<u64>(h->fn, 1);
+    for (const AdjRecord& q : h->recs) nmax = std::max<u64>(nmax, q.n_in);
+    CK(cudaMalloc(&B.abar_out, nmax * 8));
+    CK(cudaMalloc(&B.abar_in, nmax * 8));
     rc = index_dense<KW>(ctx, out, B.slots_out, B.slots_out_n, B.err);
     if (rc) return rc;
     if (h->fn)
@@ -2109,7 +2113,7 @@ int batch_adjoint(ffg_batch* h, const double* weights, double* grad_theta, doubl
         in.key = rec.key;
         in.re = rec.re;
         in.cap = n_in;
-        CK(cudaMalloc(&B.abar_in, std::max<u64>(n_in, 1) * 8));
+        if (n_in > nmax) return set_err(ctx, FFG_ERR_STATE, "adjoint: step larger than recorded");
         if (n_in && rec.type == AdjRecord::CLIFF) {
             std::vector<int2> segs;
             for (size_t o = rec.op_begin; o < rec.op_end; o++) segs.push_back(make_int2(h->ops[o].begin, h->ops[o].end));
@@ -2187,9 +2191,7 @@ int batch_adjoint(ffg_batch* h, const double* weights, double* grad_theta, doubl
         rc = index_dense<KW>(ctx, in, B.slots_in, B.slots_in_n, B.err);
         if (rc) break;
         CK(cudaStreamSynchronize(ctx->stream));
-        CK(cudaFree(B.abar_out));
-        B.abar_out = B.abar_in;
-        B.abar_in = nullptr;
+        std::swap(B.abar_out, B.abar_in);
         std::swap(B.slots_out, B.slots_in);
         std::swap(B.slots_out_n, B.slots_in_n);
         out = in;
