@@ -111,7 +111,7 @@ class KickedIsingW10(KickedIsing):
     metric = "term-gate applications/s (10x10 kicked Ising, 20 steps, W=10, tau=1e-6, theta_h=0.3)"
     thetas = (0.3,)
     maxdeg = 10
-    cpu_steps = 10
+    cpu_steps = 9
 
 
 class Hubbard:
@@ -175,7 +175,7 @@ class BatchedAnsatz:
               "forward + adjoint gradient per step)")
     kind = "batched"
     ninst, nq, layers = 256, 50, 8
-    cpu_instances = 16
+    cpu_instances = 96
 
     def tables(self):
         import fastfermion_gb300 as ff
