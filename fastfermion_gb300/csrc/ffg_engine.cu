@@ -861,9 +861,10 @@ struct Engine {
         constexpr int NWo = PAULI ? NW : 1;
         const size_t tb = block_table_bytes<KW, CPLX>();
         const size_t tt = block_table_bytes<KW, CPLX, kTeamCap>();
-        static bool attr_set = false;
+        // function attributes are set once per device (bit `device` of attr_devs)
+        static u64 attr_devs = 0;
         static int team_per_sm = 1;
-        if (!attr_set) {
+        if (!((attr_devs >> (ctx->device & 63)) & 1ull)) {
             CK(cudaFuncSetAttribute(orbit_process_big<NWo, CPLX, true>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb));
             CK(cudaFuncSetAttribute(orbit_process_big<NWo, CPLX, true, 256, kTeamCap>,
@@ -871,7 +872,7 @@ struct Engine {
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                 &team_per_sm, orbit_process_big<NWo, CPLX, true, 256, kTeamCap>, 256, tt));
             team_per_sm = std::max(team_per_sm, 1);
-            attr_set = true;
+            attr_devs |= 1ull << (ctx->device & 63);
         }
         BigPool bp{};
         const u32* nbig_dev = &oc->nbig;
@@ -1029,11 +1030,11 @@ struct Engine {
     int exec_orbit_window(const OrbitJob* jobs, int njobs, int maxdeg) {
         constexpr int NWo = PAULI ? NW : 1;
         const size_t smem = sizeof(OrbitTable<KW, CPLX>) * kOrbitWarps;
-        static bool attr_set = false;
-        if (!attr_set) {
+        static u64 attr_devs = 0;  // devices whose function attributes are set
+        if (!((attr_devs >> (ctx->device & 63)) & 1ull)) {
             CK(cudaFuncSetAttribute(orbit_process<NWo, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
-            attr_set = true;
+            attr_devs |= 1ull << (ctx->device & 63);
         }
         const int G = ctx->num_sms * 8;
         // qubit -> gate indexes of every job (Pauli batches), uploaded once
@@ -1293,9 +1294,9 @@ struct Engine {
         const size_t wsm = (size_t)kMWarps * mtable_bytes<KW>(kMWarpCap);
         const size_t tsm = mtable_bytes<KW>(kMTeamCap);
         const size_t ssm = (size_t)(32 * kMSubWarps / kMSubLanes) * mtable_bytes<KW>(kMSubCap);
-        static bool attr_set = false;
+        static u64 attr_devs = 0;  // devices whose function attributes are set
         static int team_per_sm = 1, sub_per_sm = 1;
-        if (!attr_set) {
+        if (!((attr_devs >> (ctx->device & 63)) & 1ull)) {
             CK(cudaFuncSetAttribute(morbit_sub<KW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sub_per_sm, morbit_sub<KW>, 32 * kMSubWarps, ssm));
             sub_per_sm = std::max(sub_per_sm, 1);
@@ -1304,7 +1305,7 @@ struct Engine {
                                     (int)tsm));
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&team_per_sm, morbit_block<KW, 256, true>, 256, tsm));
             team_per_sm = std::max(team_per_sm, 1);
-            attr_set = true;
+            attr_devs |= 1ull << (ctx->device & 63);
         }
         u64 out_cap = std::max<u64>(cap, pow2_at_least(4 * n_in));
         const int G = ctx->num_sms * 8;
