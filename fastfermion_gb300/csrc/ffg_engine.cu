@@ -1272,12 +1272,41 @@ struct Engine {
             g.odd = rots[i].gate_odd;
             mg[i] = g;
         }
+        h_mgates = mg;
         return upload(ctx->d_mgates, ctx->mgates_cap, mg);
     }
 
     // Gates [g0, g0 + k) of the Majorana gate table (application order), all
     // mutually commuting, each followed by the threshold of t, on the dense
     // live store.
+    std::vector<MBatchGate> h_mgates;  // host copy of the Majorana gate table
+
+    // mode -> gate index of gates [g0, g0 + k) (MOrbitArgs::midx layout); empty
+    // when some gate has odd degree
+    bool build_midx(int g0, int k, std::vector<u32>& out) const {
+        std::vector<std::vector<u32>> lists(256);
+        for (int t = 0; t < k; t++) {
+            const MBatchGate& G = h_mgates[g0 + t];
+            if (G.odd) return false;
+            for (int w = 0; w < 4; w++) {
+                u64 sup = G.p[w];
+                while (sup) {
+                    lists[64 * w + __builtin_ctzll(sup)].push_back((u32)t);
+                    sup &= sup - 1;
+                }
+            }
+        }
+        out.assign(257, 0);
+        u32 e = 0;
+        for (int i = 0; i < 256; i++) {
+            out[i] = e;
+            e += (u32)lists[i].size();
+        }
+        out[256] = e;
+        for (int i = 0; i < 256; i++) out.insert(out.end(), lists[i].begin(), lists[i].end());
+        return true;
+    }
+
     int exec_morbit_batch(int g0, int k, const TruncArgs& t, int maxdeg) {
         const u64 n_in = ctx->h_ctr->n;
         if (n_in == 0) return FFG_OK;
@@ -1291,6 +1320,14 @@ struct Engine {
         a.thr = t.thr;
         a.tau = t.tau;
         a.route_big = ctx->orbit_route_big;
+        if (ctx->orbit_qidx) {
+            std::vector<u32> mv;
+            if (build_midx(g0, k, mv)) {
+                int rc = upload(ctx->d_qidx, ctx->qidx_cap, mv);
+                if (rc) return rc;
+                a.midx = ctx->d_qidx;
+            }
+        }
         const size_t wsm = (size_t)kMWarps * mtable_bytes<KW>(kMWarpCap);
         const size_t tsm = mtable_bytes<KW>(kMTeamCap);
         const size_t ssm = (size_t)(32 * kMSubWarps / kMSubLanes) * mtable_bytes<KW>(kMSubCap);

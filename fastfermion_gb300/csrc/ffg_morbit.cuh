@@ -42,6 +42,10 @@ struct MOrbitArgs {
     int thr;                  // threshold after every gate
     double tau;
     int route_big;            // groups with at least this many gates skip the warp tier
+    // mode -> gates index of the run when every gate has even degree (null
+    // otherwise): an even string anticommutes only with strings that overlap
+    // it.  Gates touching mode i are midx[257 + midx[i] .. 257 + midx[i + 1]).
+    const u32* midx;
 };
 
 template <int KW>
@@ -77,11 +81,33 @@ __global__ void __launch_bounds__(kBlock) morbit_classify(StoreView in, StoreVie
         load_key<KW>(in, i, q);
         u64 A[kAW] = {};
         u64 U[KW] = {};
-        for (int t = 0; t < a.k; t++) {
-            if (manti<KW>(q, gp[t], godd[t])) {
-                A[t >> 6] |= 1ull << (t & 63);
+        if (a.midx) {
+            // candidates: the gates on the string's modes
 #pragma unroll
-                for (int w = 0; w < KW; w++) U[w] |= gp[t][w];
+            for (int ws = 0; ws < KW; ws++) {
+                u64 sup = q[ws];
+                while (sup) {
+                    const int md = 64 * ws + __ffsll((long long)sup) - 1;
+                    sup &= sup - 1;
+                    const u32 e1 = __ldg(&a.midx[md + 1]);
+                    for (u32 e = __ldg(&a.midx[md]); e < e1; e++) {
+                        const int t = (int)__ldg(&a.midx[257 + e]);
+                        if ((A[t >> 6] >> (t & 63)) & 1ull) continue;
+                        if (manti<KW>(q, gp[t], 0)) {
+                            A[t >> 6] |= 1ull << (t & 63);
+#pragma unroll
+                            for (int w = 0; w < KW; w++) U[w] |= gp[t][w];
+                        }
+                    }
+                }
+            }
+        } else {
+            for (int t = 0; t < a.k; t++) {
+                if (manti<KW>(q, gp[t], godd[t])) {
+                    A[t >> 6] |= 1ull << (t & 63);
+#pragma unroll
+                    for (int w = 0; w < KW; w++) U[w] |= gp[t][w];
+                }
             }
         }
         bool any = false;
