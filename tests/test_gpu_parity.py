@@ -98,3 +98,87 @@ def test_sort_merge_path_matches_reference(name):
         assert checksum(keys, re, im) == str(fx["checksum"])
     finally:
         ctx.set_option("merge_sort", 0)
+
+
+def _all_pauli_strings(nq):
+    """Every non-identity Pauli string on nq qubits as (4, 4^nq - 1) key planes."""
+    keys = []
+    for code in range(1, 4 ** nq):
+        x = z = 0
+        for q in range(nq):
+            p = (code >> (2 * q)) & 3  # 1 X, 2 Y, 3 Z
+            if p in (1, 2):
+                x |= 1 << q
+            if p in (2, 3):
+                z |= 1 << q
+        keys.append((x, 0, z, 0))
+    return np.array(keys, dtype=np.uint64).T.copy()
+
+
+@pytest.mark.parametrize("batched", [True, False])
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_exhaustive_three_qubit_pauli(seed, batched):
+    """All 63 non-identity strings on 3 qubits with random complex coefficients
+    through a random circuit of every gate type: GPU == oracle, bit for bit."""
+    from fastfermion_gb300 import _native
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    keys = _all_pauli_strings(3)
+    n = keys.shape[1]
+    re, im = rng.normal(size=n), rng.normal(size=n) * (seed % 2)
+    table = np.zeros(40, dtype=_native.PAULI_GATE)
+    for i in range(40):
+        kind = int(rng.integers(0, 6)) if rng.random() < 0.4 else 0
+        table[i]["kind"] = kind
+        if kind == 0:
+            x = int(rng.integers(0, 8))
+            z = int(rng.integers(0, 8))
+            table[i]["x"] = (x, 0)
+            table[i]["z"] = (z, 0)
+            table[i]["theta"] = rng.uniform(-3, 3)
+        else:
+            a, b = rng.choice(3, 2, replace=False)
+            table[i]["q0"], table[i]["q1"] = int(a), int(b)
+    md = int(rng.integers(1, 4))
+    p = dict(maxdegree=md, topk=0, mincoeff=1e-3 if seed == 2 else 0.0, max_xweight=-1, xtrunc_period=1,
+             batched=int(batched), deterministic=0)
+    g = _native.context(0).pauli_propagate(keys, re, im, table, dict(p))
+    o = O.pauli_propagate(table, keys, re, im, maxdegree=md, mincoeff=p["mincoeff"], batched=batched)
+    assert_same_terms(g.copy(), (o.keys, o.re, o.im))
+
+
+@pytest.mark.parametrize("seed", [4, 5])
+def test_exhaustive_four_mode_majorana(seed):
+    """All 15 non-empty Majorana strings on 4 modes through random MROT
+    circuits (odd and even degree): GPU == oracle, bit for bit."""
+    from fastfermion_gb300 import _native
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    keys = np.zeros((4, 15), dtype=np.uint64)
+    keys[0] = np.arange(1, 16, dtype=np.uint64)
+    re, im = rng.normal(size=15), rng.normal(size=15)
+    table = np.zeros(30, dtype=_native.MAJORANA_GATE)
+    for i in range(30):
+        a = int(rng.integers(1, 16))
+        table[i]["alpha"] = (a, 0, 0, 0)
+        table[i]["theta"] = rng.uniform(-2, 2)
+        deg = bin(a).count("1")
+        table[i]["r"] = 0 if deg % 4 in (0, 1) else 1
+    pm = dict(has_maxdegree=1, maxdegree=3, mincoeff=1e-3, deterministic=0, pad=0)
+    g = _native.context(0).majorana_propagate(keys, re, im, table, dict(pm))
+    o = O.majorana_propagate(table, keys, re, im, maxdegree=3, mincoeff=1e-3)
+    assert_same_terms(g.copy(), (o.keys, o.re, o.im))
+
+
+def test_large_results_have_distinct_keys():
+    """Size-independent invariants of large results: distinct keys (the merge
+    left no duplicate), finite coefficients, above the threshold."""
+    for name in ("cfg2_kicked_ising_0p5000", "hubbard_6x6_10steps", "cfg2w10_kicked_ising_0p3000"):
+        fx = load(name)
+        keys, re, im = run_gpu(fx).copy()
+        k = np.ascontiguousarray(keys.T).view(np.dtype((np.void, 32))).ravel()
+        assert np.unique(k).size == k.size, name
+        assert np.all(np.isfinite(re)) and np.all(np.isfinite(im)), name
+        tau = float(fx["mincoeff"])
+        if tau > 0:
+            assert np.all(np.hypot(re, im) > tau), name
