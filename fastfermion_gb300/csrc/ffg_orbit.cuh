@@ -128,11 +128,11 @@ __device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol
 // barrier of a team of TEAM threads (a warp, or the whole block)
 template <int TEAM>
 __device__ __forceinline__ void team_sync() {
-    if (TEAM < 32) {
+    if constexpr (TEAM < 32) {
         // the TEAM-lane slice of the warp that this thread belongs to
         const unsigned lane = threadIdx.x & 31;
         __syncwarp(((1u << TEAM) - 1) << (lane & ~(unsigned)(TEAM - 1)));
-    } else if (TEAM == 32) {
+    } else if constexpr (TEAM == 32) {
         __syncwarp();
     } else {
         __syncthreads();
