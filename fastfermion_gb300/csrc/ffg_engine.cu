@@ -183,6 +183,8 @@ struct ffg_ctx {
     bool orbit_qidx = true;     // classify against the gates on each term's support (FFG_ORBIT_QIDX=0 disables)
     int orbit_window = kOrbitWindowMax;  // orbit batches per host round trip (1..kOrbitWindowMax)
     bool merge_sort = false;    // per-gate sort-and-reduce merge instead of the hash / orbit paths
+    int orbit_team_threads = 256;   // threads of a team-tier group (128 or 256)
+    int orbit_block_threads = 1024; // threads of a block-tier group (512 or 1024)
     void* d_smscratch = nullptr;
     size_t smscratch_bytes = 0;
     int morbit_min_gates = 2;   // shortest Majorana run sent to the batch-orbit path
@@ -861,19 +863,28 @@ struct Engine {
         constexpr int NWo = PAULI ? NW : 1;
         const size_t tb = block_table_bytes<KW, CPLX>();
         const size_t tt = block_table_bytes<KW, CPLX, kTeamCap>();
+        // the tier kernels at each thread count (options orbit_team_threads, orbit_block_threads)
+        auto team_k = ctx->orbit_team_threads == 128 ? orbit_process_big<NWo, CPLX, true, 128, kTeamCap>
+                                                     : orbit_process_big<NWo, CPLX, true, 256, kTeamCap>;
+        auto block_k = ctx->orbit_block_threads == 512 ? orbit_process_big<NWo, CPLX, true, 512, kBlockCap>
+                                                       : orbit_process_big<NWo, CPLX, true, 1024, kBlockCap>;
         // function attributes are set once per device (bit `device` of attr_devs)
         static u64 attr_devs = 0;
         static int team_per_sm = 1;
         if (!((attr_devs >> (ctx->device & 63)) & 1ull)) {
-            CK(cudaFuncSetAttribute(orbit_process_big<NWo, CPLX, true>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb));
-            CK(cudaFuncSetAttribute(orbit_process_big<NWo, CPLX, true, 256, kTeamCap>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tt));
+            for (auto k : {orbit_process_big<NWo, CPLX, true, 512, kBlockCap>,
+                           orbit_process_big<NWo, CPLX, true, 1024, kBlockCap>})
+                CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb));
+            for (auto k : {orbit_process_big<NWo, CPLX, true, 128, kTeamCap>,
+                           orbit_process_big<NWo, CPLX, true, 256, kTeamCap>})
+                CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tt));
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                 &team_per_sm, orbit_process_big<NWo, CPLX, true, 256, kTeamCap>, 256, tt));
             team_per_sm = std::max(team_per_sm, 1);
             attr_devs |= 1ull << (ctx->device & 63);
         }
+        const int tthreads = ctx->orbit_team_threads == 128 ? 128 : 256;
+        const int bthreads = ctx->orbit_block_threads == 512 ? 512 : 1024;
         BigPool bp{};
         const u32* nbig_dev = &oc->nbig;
         PhaseScope ps(ctx, PH_ROT);
@@ -881,19 +892,19 @@ struct Engine {
             // sc.big -> retry_list (count nretry[0]) -> sc.big (count nretry[1])
             bp.retry = retry_list;
             bp.nretry = nretry;
-            CK(launch_k(ctx->pdl, orbit_process_big<NWo, CPLX, true, 256, kTeamCap>, ctx->num_sms * team_per_sm, 256,
-                        tt, ctx->stream, in, out, sc, oc, a, bp, (const u32*)sc.big, 0u, nbig_dev));
+            CK(launch_k(ctx->pdl, team_k, ctx->num_sms * team_per_sm, tthreads, tt, ctx->stream, in, out, sc, oc, a,
+                        bp, (const u32*)sc.big, 0u, nbig_dev));
             bp.retry = sc.big;
             bp.nretry = nretry + 1;
-            CK(launch_k(ctx->pdl, orbit_process_big<NWo, CPLX, true>, ctx->num_sms, 1024, tb, ctx->stream, in, out, sc,
-                        oc, a, bp, (const u32*)retry_list, 0u, (const u32*)nretry));
+            CK(launch_k(ctx->pdl, block_k, ctx->num_sms, bthreads, tb, ctx->stream, in, out, sc, oc, a, bp,
+                        (const u32*)retry_list, 0u, (const u32*)nretry));
             ctx->prof.kernel_launches += 2;
         } else {
             // sc.big -> retry_list (count nretry[1])
             bp.retry = retry_list;
             bp.nretry = nretry + 1;
-            CK(launch_k(ctx->pdl, orbit_process_big<NWo, CPLX, true>, ctx->num_sms, 1024, tb, ctx->stream, in, out, sc,
-                        oc, a, bp, (const u32*)sc.big, 0u, nbig_dev));
+            CK(launch_k(ctx->pdl, block_k, ctx->num_sms, bthreads, tb, ctx->stream, in, out, sc, oc, a, bp,
+                        (const u32*)sc.big, 0u, nbig_dev));
             ctx->prof.kernel_launches++;
         }
         OSTEP("orbit_process_big");
@@ -2287,6 +2298,8 @@ int ffg_create(ffg_ctx** out, int device) {
     if (const char* d = getenv("FFG_MORBIT")) ctx->morbit = atoi(d) != 0;
     if (const char* d = getenv("FFG_PDL")) ctx->pdl = atoi(d) != 0;
     if (const char* d = getenv("FFG_ORBIT_QIDX")) ctx->orbit_qidx = atoi(d) != 0;
+    if (const char* d = getenv("FFG_TEAM_THREADS")) ctx->orbit_team_threads = atoi(d) == 128 ? 128 : 256;
+    if (const char* d = getenv("FFG_BLOCK_THREADS")) ctx->orbit_block_threads = atoi(d) == 512 ? 512 : 1024;
     if (const char* d = getenv("FFG_MORBIT_MIN")) ctx->morbit_min_gates = std::max(1, atoi(d));
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
@@ -3211,6 +3224,10 @@ const OptionRef kOptions[] = {
     {"pdl", [](const ffg_ctx* c) { return (int)c->pdl; }, [](ffg_ctx* c, int64_t v) { c->pdl = v != 0; return true; }},
     {"morbit", [](const ffg_ctx* c) { return (int)c->morbit; },
      [](ffg_ctx* c, int64_t v) { c->morbit = v != 0; return true; }},
+    {"orbit_team_threads", [](const ffg_ctx* c) { return c->orbit_team_threads; },
+     [](ffg_ctx* c, int64_t v) { if (v != 128 && v != 256) return false; c->orbit_team_threads = (int)v; return true; }},
+    {"orbit_block_threads", [](const ffg_ctx* c) { return c->orbit_block_threads; },
+     [](ffg_ctx* c, int64_t v) { if (v != 512 && v != 1024) return false; c->orbit_block_threads = (int)v; return true; }},
     {"merge_sort", [](const ffg_ctx* c) { return (int)c->merge_sort; },
      [](ffg_ctx* c, int64_t v) { c->merge_sort = v != 0; return true; }},
     {"morbit_min_gates", [](const ffg_ctx* c) { return c->morbit_min_gates; },

@@ -132,7 +132,9 @@ void* ffg_stream(const ffg_ctx* ctx);
 /* Engine options (no counterpart in the reference): runtime knobs of the
  * orbit engine, tuned by fastfermion_gb300.autotune.  Names:
  *   orbit_route_big   |A| from which a Pauli group skips the warp tier (default 8)
- *   orbit_team        1: 256-thread team tier before the 1024-thread tier (1)
+ *   orbit_team        1: team tier (1024-member tables) before the block tier (1)
+ *   orbit_team_threads   threads per team-tier group: 128 or 256 (256)
+ *   orbit_block_threads  threads per block-tier group: 512 or 1024 (1024)
  *   orbit_window      orbit batches per host round trip, 1..16 (16)
  *   orbit_min_gates   shortest commuting run sent to the orbit path (4)
  *   orbit_qidx        1: classify against the gates on each term's support (1)
