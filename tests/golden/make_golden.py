@@ -290,7 +290,7 @@ def cases(ff):
         for oi, o in enumerate(obss):
             nm = f"ref_circuit_{ci}_{oi}"
             yield nm, (lambda nm=nm, c=c, o=o: pauli_case(ff, nm, c, ff.poly(o)))
-    # BASELINE configs
+    # the benchmark configurations (16-qubit chain, 10x10 kicked Ising)
     yield "cfg1_chain", lambda: pauli_case(ff, "cfg1_chain", [mk(ff, s) for s in W.chain_circuit()], P("Z7"), maxdegree=6, mincoeff=1e-8, states=((0, 0), (0b1010110011, 0)))
     yield "cfg1_chain_unbatched", lambda: pauli_case(ff, "cfg1_chain_unbatched", [mk(ff, s) for s in W.chain_circuit()], P("Z7"), maxdegree=6, mincoeff=1e-8, batched=False)
     for th in W.KICKED_ISING_THETAS:
