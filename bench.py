@@ -58,6 +58,7 @@ class KickedIsing:
     thetas = (0.1, 0.3, 0.5, 0.7, 0.9, 1.1, math.pi / 2)
     maxdeg = MAXDEG
     cpu_steps = 20  # Trotter steps of each propagation in the CPU sample
+    serial_steps = 20  # Trotter steps of the one-core sample (about 8 s)
 
     @property
     def params(self):
@@ -99,6 +100,18 @@ class KickedIsing:
             f"{sweeps} x the theta_h sweep of the same workload{part}, sharded OpenMP port "
             "of the reference algorithm")
 
+    def serial_sample(self):
+        """The oracle's serial port (one core, the reference's parallel="serial"
+        strategy) on the first theta_h of the sweep, first serial_steps Trotter steps."""
+        from oracle import oracle as O
+        keys, re, im = self.observable()
+        tab = self.tables(self.serial_steps)[0]
+        t0 = time.perf_counter()
+        apps = O.pauli_propagate(tab, keys, re, im, maxdegree=self.maxdeg, mincoeff=TAU, n_threads=1).apps
+        part = "" if self.serial_steps == 20 else f", first {self.serial_steps} of 20 Trotter steps"
+        return apps, time.perf_counter() - t0, (
+            f"theta_h={self.thetas[0]:.6g}{part}, serial port of the reference algorithm")
+
     def config(self):
         return {"workload": self.name, "lattice": "10x10 open", "trotter_steps": 20,
                 "maxdegree": self.maxdeg, "mincoeff": TAU, "theta_h": [round(t, 6) for t in self.thetas],
@@ -113,6 +126,7 @@ class KickedIsingW10(KickedIsing):
     thetas = (0.3,)
     maxdeg = 10
     cpu_steps = 9
+    serial_steps = 3
 
 
 class Hubbard:
@@ -340,8 +354,13 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 def cpu_baseline(wl, tabs):
     apps, dt, cores, desc = wl.cpu_sample(tabs, os.cpu_count() or 1, min_seconds=10.0)
-    return {"value": apps / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{desc} ({apps} apps, {dt:.1f} s)"}
+    out = {"value": apps / dt, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{desc} ({apps} apps, {dt:.1f} s)"}
+    if hasattr(wl, "serial_sample"):
+        apps, dt, desc = wl.serial_sample()
+        out["serial"] = {"value": apps / dt, "unit": UNIT, "cores": 1,
+                         "sample": f"{desc} ({apps} apps, {dt:.1f} s)"}
+    return out
 
 
 def run_reference(args):
