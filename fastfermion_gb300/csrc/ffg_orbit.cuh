@@ -14,17 +14,24 @@
 // rather than with (gates x store size).
 //
 // Kernels of one batch:
+//   orbit_gate       opens the batch: input size from the previous batch's
+//                    counters, or skip when that batch did not complete
 //   orbit_classify   A(Q) and the group key of every input term; terms with
 //                    A = {} are final and go straight to the output store
 //   orbit_group      representative of every term's group (hash of the key)
-//   orbit_count / orbit_offsets / orbit_scatter
-//                    group members made contiguous
+//   orbit_offsets / orbit_scatter
+//                    group ranges, members (keys, coefficients) copied into
+//                    group order
 //   orbit_process    one warp per group: members in a shared-memory table,
 //                    gates applied in order, survivors of the batch-end
 //                    truncation appended to the output store
-// A group whose member count would exceed kOrbitCap stops the batch (the
-// host falls back to per-gate passes for it); so does an output store that
-// would overflow (the host grows it and runs the batch again).
+//   orbit_process_big
+//                    groups that outgrow a warp table, or whose |A| reaches
+//                    the routing threshold: a thread team with a larger
+//                    shared-memory table, then a block with a global-memory
+//                    region
+// An output store that would overflow stops the batch (the host grows it and
+// runs the batch again from its intact input).
 #pragma once
 #include "ffg_kernels.cuh"
 
