@@ -144,7 +144,8 @@ class Context:
             raise FFGError(f"libffg error {rc}: {msg}")
 
     OPTIONS = ("orbit_route_big", "orbit_team", "orbit_window", "orbit_min_gates", "orbit_qidx", "pdl",
-               "morbit", "morbit_min_gates", "merge_sort", "orbit_team_threads", "orbit_block_threads")
+               "morbit", "morbit_min_gates", "morbit_route_big", "merge_sort", "orbit_team_threads",
+               "orbit_block_threads")
 
     def set_option(self, name, value):
         self.check(self.L.ffg_set_option(self.h, name.encode(), int(value)))

@@ -1,9 +1,11 @@
 """Autotuner for the orbit engine's runtime options.
 
 The engine's tuning knobs (``ffg_set_option``): the |A| threshold from which
-a group skips the warp tier (``orbit_route_big``), the 256-thread team tier
-(``orbit_team``), orbit batches per host round trip (``orbit_window``) and
-programmatic dependent launch (``pdl``).  ``autotune`` times a propagation of
+a group skips the warp tier (``orbit_route_big`` for Pauli circuits,
+``morbit_route_big`` for Majorana circuits), the 256-thread team tier
+(``orbit_team``), orbit batches per host round trip (``orbit_window``),
+programmatic dependent launch (``pdl``) and, for Majorana circuits, the
+shortest commuting run sent to the orbit path (``morbit_min_gates``).  ``autotune`` times a propagation of
 the caller's own circuit and observable under candidate settings (coordinate
 descent over the space, best of ``repeats`` runs each), keeps the fastest
 setting on the device's context and caches it per circuit, observable and
@@ -24,7 +26,20 @@ DEFAULT_SPACE = {
     "pdl": (1, 0),
 }
 
+MAJORANA_SPACE = {
+    "morbit_route_big": (12, 8, 10, 16),
+    "morbit_min_gates": (2, 1, 4),
+    "orbit_team": (1, 0),
+    "orbit_window": (16, 4),
+    "pdl": (1, 0),
+}
+
 _cache = {}
+
+
+def _is_majorana(circuit):
+    from .majorana import MROT
+    return len(circuit) > 0 and all(isinstance(g, MROT) for g in circuit)
 
 
 def _signature(circuit, observable, kwargs):
@@ -59,7 +74,9 @@ def autotune(circuit, observable, space=None, repeats=2, device=None, **kwargs):
         for k, v in _cache[key]["options"].items():
             ctx.set_option(k, v)
         return _cache[key]
-    space = dict(DEFAULT_SPACE if space is None else space)
+    if space is None:
+        space = MAJORANA_SPACE if _is_majorana(circuit) else DEFAULT_SPACE
+    space = dict(space)
     kwargs = dict(kwargs)
     if device is not None:
         kwargs["device"] = device

@@ -188,6 +188,8 @@ struct ffg_ctx {
     void* d_smscratch = nullptr;
     size_t smscratch_bytes = 0;
     int morbit_min_gates = 2;   // shortest Majorana run sent to the batch-orbit path
+    int morbit_route_big = 12;  // |A| from which a Majorana group skips the warp tier (FFG_MORBIT_ROUTE);
+                                // 6x6 Hubbard: 323 ms at 12 or 16, 329 ms at 10, 356 ms at 8
     MBatchGate* d_mgates = nullptr;
     size_t mgates_cap = 0;
     u32* d_qidx = nullptr;      // qubit -> gate indexes of the orbit batches of a window call
@@ -1330,7 +1332,7 @@ struct Engine {
         a.maxdeg = maxdeg;
         a.thr = t.thr;
         a.tau = t.tau;
-        a.route_big = ctx->orbit_route_big;
+        a.route_big = ctx->morbit_route_big;
         if (ctx->orbit_qidx) {
             std::vector<u32> mv;
             if (build_midx(g0, k, mv)) {
@@ -2301,6 +2303,7 @@ int ffg_create(ffg_ctx** out, int device) {
     if (const char* d = getenv("FFG_TEAM_THREADS")) ctx->orbit_team_threads = atoi(d) == 128 ? 128 : 256;
     if (const char* d = getenv("FFG_BLOCK_THREADS")) ctx->orbit_block_threads = atoi(d) == 512 ? 512 : 1024;
     if (const char* d = getenv("FFG_MORBIT_MIN")) ctx->morbit_min_gates = std::max(1, atoi(d));
+    if (const char* d = getenv("FFG_MORBIT_ROUTE")) ctx->morbit_route_big = std::max(1, atoi(d));
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -3232,6 +3235,8 @@ const OptionRef kOptions[] = {
      [](ffg_ctx* c, int64_t v) { c->merge_sort = v != 0; return true; }},
     {"morbit_min_gates", [](const ffg_ctx* c) { return c->morbit_min_gates; },
      [](ffg_ctx* c, int64_t v) { if (v < 1) return false; c->morbit_min_gates = (int)v; return true; }},
+    {"morbit_route_big", [](const ffg_ctx* c) { return c->morbit_route_big; },
+     [](ffg_ctx* c, int64_t v) { if (v < 1 || v > 1 << 20) return false; c->morbit_route_big = (int)v; return true; }},
 };
 }  // namespace
 

@@ -141,6 +141,7 @@ void* ffg_stream(const ffg_ctx* ctx);
  *   pdl               1: programmatic dependent launch of the orbit kernels (1)
  *   morbit            1: orbit path for commuting Majorana runs (1)
  *   morbit_min_gates  shortest Majorana run sent to the orbit path (2)
+ *   morbit_route_big  |A| from which a Majorana group skips the warp tier (12)
  *   merge_sort        1: Pauli rotations one at a time with a radix sort and a
  *                     segmented reduce instead of the hash index / orbit paths (0)
  * Results do not depend on the options (only speed does). */

@@ -109,6 +109,16 @@ def test_reference_quirk_unknown_strategy_returns_input():
     assert len(r) == 1
 
 
+def test_autotune_space_follows_the_circuit_kind():
+    from fastfermion_gb300.autotune import DEFAULT_SPACE, MAJORANA_SPACE, _is_majorana
+    from fastfermion_gb300 import _native
+    assert _is_majorana(ff.build_circuit(ff.workloads.hubbard_circuit(2, 2, steps=1)))
+    assert not _is_majorana(ff.build_circuit(ff.workloads.kicked_ising_circuit(0.5, 3, 3, 1)))
+    assert not _is_majorana([])
+    for space in (DEFAULT_SPACE, MAJORANA_SPACE):
+        assert set(space) <= set(_native.Context.OPTIONS)
+
+
 @pytest.mark.gpu
 def test_engine_options_and_autotune():
     """Options change speed only; the tuner checks that and keeps the fastest."""

@@ -100,6 +100,29 @@ def test_sort_merge_path_matches_reference(name):
         ctx.set_option("merge_sort", 0)
 
 
+MAJORANA_ROUTE = [n for n in EXACT if str(load(n)["kind"]) == "majorana" and float(load(n)["ref_seconds"]) < 30.0]
+
+
+@pytest.mark.parametrize("route", [1, 4, 8, 16, 1 << 20])
+def test_majorana_routing_threshold_keeps_results(route):
+    """Every |A| routing threshold of the Majorana orbit path (which groups the
+    warp tier takes and which go straight to the team and block tiers) gives
+    the reference's term sets bit for bit."""
+    from fastfermion_gb300 import _native
+    ctx = _native.context(0)
+    before = ctx.get_option("morbit_route_big")
+    ctx.set_option("morbit_route_big", route)
+    try:
+        for name in MAJORANA_ROUTE:
+            fx = load(name)
+            r = run_gpu(fx)
+            keys, re, im = r.copy()
+            assert r.n == int(fx["n_terms"]), name
+            assert checksum(keys, re, im) == str(fx["checksum"]), name
+    finally:
+        ctx.set_option("morbit_route_big", before)
+
+
 def _all_pauli_strings(nq):
     """Every non-identity Pauli string on nq qubits as (4, 4^nq - 1) key planes."""
     keys = []
