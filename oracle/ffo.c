@@ -270,7 +270,27 @@ static int clifford_apply(const ffo_pauli_gate* g, uint64_t* k) {
 /* Pauli rotation, serial (src/pauli/propagate.h:71-89)                      */
 /* ------------------------------------------------------------------------- */
 
-static void pauli_conjugate(map_t* m, const ffo_pauli_gate* g, int maxdeg, vec_t* nb) {
+/* Partners dropped by the degree filter, recorded for the learned-correction
+ * form's training data (not a reference feature): key, coefficient and the
+ * index of the gate that created them, for degrees up to capdeg. */
+struct ffo_drops {
+    vec_t t;
+    int64_t* gate;
+    int64_t gcap;
+    int capdeg;
+};
+
+static void drops_push(ffo_drops* d, const term_t* p, int64_t gi) {
+    vec_push(&d->t, p);
+    if (d->t.n > d->gcap) {
+        d->gcap = d->t.cap;
+        d->gate = (int64_t*)realloc(d->gate, (size_t)d->gcap * sizeof(int64_t));
+    }
+    d->gate[d->t.n - 1] = gi;
+}
+
+static void pauli_conjugate(map_t* m, const ffo_pauli_gate* g, int maxdeg, vec_t* nb, ffo_drops* drops,
+                            int64_t gi) {
     const double c = cos(g->theta);
     const double s = sin(g->theta);
     nb->n = 0;
@@ -279,12 +299,16 @@ static void pauli_conjugate(map_t* m, const ffo_pauli_gate* g, int maxdeg, vec_t
         if (!pauli_anticommutes(t->k, g->x, g->z)) continue;
         term_t p;
         int jpow = pauli_mul(g->x, g->z, t->k, p.k);
-        if (pauli_degree(p.k) <= maxdeg) {
+        const int deg = pauli_degree(p.k);
+        if (deg <= maxdeg || (drops && deg <= drops->capdeg)) {
             double tr, ti, fr, fi;
             cmul(t->re, t->im, 0.0, s, &tr, &ti); /* coeff * (i sin) */
             ipow(jpow, &fr, &fi);
             cmul(tr, ti, fr, fi, &p.re, &p.im); /* ... * phase(P*Q) */
-            vec_push(nb, &p);
+            if (deg <= maxdeg)
+                vec_push(nb, &p);
+            else
+                drops_push(drops, &p, gi);
         }
         t->re = t->re * c;
         t->im = t->im * c;
@@ -470,6 +494,7 @@ typedef struct {
     vec_t nb;
     int rot_count;
     int64_t apps, peak;
+    ffo_drops* drops; /* serial strategy only */
 } pdrv_t;
 
 static int64_t drv_size(pdrv_t* D) { return D->S ? shards_size(D->S) : D->m->d.n; }
@@ -479,7 +504,7 @@ static void drv_rot(pdrv_t* D, int64_t gi) {
     if (D->S)
         pauli_conjugate_sharded(D->S, &D->gates[gi], D->p->maxdegree);
     else
-        pauli_conjugate(D->m, &D->gates[gi], D->p->maxdegree, &D->nb);
+        pauli_conjugate(D->m, &D->gates[gi], D->p->maxdegree, &D->nb, D->drops, gi);
     int64_t n = drv_size(D);
     if (n > D->peak) D->peak = n;
 }
@@ -530,9 +555,9 @@ static void drv_flush(pdrv_t* D, int64_t* buf, int64_t* nbuf) {
 
 static int valid_qubit(int q) { return q >= 0 && q < 128; }
 
-ffo_poly* ffo_pauli_propagate(const ffo_pauli_gate* gates, int64_t ngates, const uint64_t* keys,
-                              const double* re, const double* im, int64_t n,
-                              const ffo_pauli_params* p) {
+static ffo_poly* pauli_propagate(const ffo_pauli_gate* gates, int64_t ngates, const uint64_t* keys,
+                                 const double* re, const double* im, int64_t n, const ffo_pauli_params* p,
+                                 ffo_drops* drops) {
     for (int64_t i = 0; i < ngates; i++) {
         const ffo_pauli_gate* g = &gates[i];
         if (g->kind < 0 || g->kind > FFO_CZ) return NULL;
@@ -547,11 +572,12 @@ ffo_poly* ffo_pauli_propagate(const ffo_pauli_gate* gates, int64_t ngates, const
         uint64_t k[4] = {keys[i], keys[n + i], keys[2 * n + i], keys[3 * n + i]};
         map_add(&out->m, k, re[i], im ? im[i] : 0.0);
     }
-    int T = p->n_threads > 1 ? p->n_threads : 1;
+    int T = p->n_threads > 1 && !drops ? p->n_threads : 1;
     shards_t S = {0};
     pdrv_t D = {0};
     D.gates = gates;
     D.p = p;
+    D.drops = drops;
     D.m = &out->m;
     D.peak = out->m.d.n;
     if (T > 1) {
@@ -615,6 +641,46 @@ ffo_poly* ffo_pauli_propagate(const ffo_pauli_gate* gates, int64_t ngates, const
     out->apps = D.apps;
     out->peak = D.peak;
     return out;
+}
+
+ffo_poly* ffo_pauli_propagate(const ffo_pauli_gate* gates, int64_t ngates, const uint64_t* keys,
+                              const double* re, const double* im, int64_t n,
+                              const ffo_pauli_params* p) {
+    return pauli_propagate(gates, ngates, keys, re, im, n, p, NULL);
+}
+
+ffo_poly* ffo_pauli_propagate_capture(const ffo_pauli_gate* gates, int64_t ngates, const uint64_t* keys,
+                                      const double* re, const double* im, int64_t n,
+                                      const ffo_pauli_params* p, int32_t capdeg, ffo_drops** dropped) {
+    ffo_drops* d = (ffo_drops*)calloc(1, sizeof(ffo_drops));
+    d->capdeg = capdeg;
+    ffo_poly* r = pauli_propagate(gates, ngates, keys, re, im, n, p, d);
+    if (!r) {
+        ffo_drops_free(d);
+        d = NULL;
+    }
+    *dropped = d;
+    return r;
+}
+
+int64_t ffo_drops_size(const ffo_drops* d) { return d ? d->t.n : 0; }
+
+void ffo_drops_copy(const ffo_drops* d, uint64_t* keys, double* re, double* im, int64_t* gate) {
+    const int64_t n = d->t.n;
+    for (int64_t i = 0; i < n; i++) {
+        const term_t* t = &d->t.v[i];
+        for (int w = 0; w < 4; w++) keys[w * n + i] = t->k[w];
+        re[i] = t->re;
+        im[i] = t->im;
+        gate[i] = d->gate[i];
+    }
+}
+
+void ffo_drops_free(ffo_drops* d) {
+    if (!d) return;
+    free(d->t.v);
+    free(d->gate);
+    free(d);
 }
 
 /* ------------------------------------------------------------------------- */

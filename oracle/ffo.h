@@ -57,6 +57,21 @@ ffo_poly* ffo_pauli_propagate(const ffo_pauli_gate* gates, int64_t ngates,
                               const uint64_t* keys /* [4][n] */, const double* re,
                               const double* im, int64_t n, const ffo_pauli_params* p);
 
+/* Partners that the degree filter drops (not a reference feature: training
+ * data of the learned-correction form).  ffo_pauli_propagate_capture runs the
+ * serial strategy (n_threads is ignored) and records, in creation order, every
+ * partner whose degree is above maxdegree and at most capdeg: its key, its
+ * coefficient c (i sin) phase, and the index of the gate that created it.  The
+ * part of the circuit still to be applied to it is gates [0, gate). */
+typedef struct ffo_drops ffo_drops;
+ffo_poly* ffo_pauli_propagate_capture(const ffo_pauli_gate* gates, int64_t ngates,
+                                      const uint64_t* keys, const double* re, const double* im,
+                                      int64_t n, const ffo_pauli_params* p, int32_t capdeg,
+                                      ffo_drops** dropped);
+int64_t ffo_drops_size(const ffo_drops* d);
+void ffo_drops_copy(const ffo_drops* d, uint64_t* keys /* [4][n] */, double* re, double* im,
+                    int64_t* gate);
+void ffo_drops_free(ffo_drops* d);
 /* Majorana propagation (src/majorana_propagation.h:18-55). */
 ffo_poly* ffo_majorana_propagate(const ffo_majorana_gate* gates, int64_t ngates,
                                  const uint64_t* keys, const double* re, const double* im,

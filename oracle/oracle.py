@@ -63,6 +63,13 @@ def lib():
         L.ffo_fock_state.argtypes = [vp, vp, dp, dp]
         L.ffo_abs.restype = ctypes.c_double
         L.ffo_abs.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.ffo_pauli_propagate_capture.restype = vp
+        L.ffo_pauli_propagate_capture.argtypes = [vp, i64, vp, vp, vp, i64, ctypes.POINTER(_Params),
+                                                  ctypes.c_int32, ctypes.POINTER(vp)]
+        L.ffo_drops_size.restype = i64
+        L.ffo_drops_size.argtypes = [vp]
+        L.ffo_drops_copy.argtypes = [vp, vp, vp, vp, vp]
+        L.ffo_drops_free.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -124,6 +131,42 @@ def pauli_propagate(gates, keys, re, im=None, maxdegree=128, mincoeff=0.0, topk=
     if not h:
         raise ValueError("oracle rejected the circuit")
     return OraclePoly(h)
+
+
+class Dropped:
+    """Partners dropped by the degree filter: keys (4, m), re, im and gate (the
+    index of the gate that created each one; gates [0, gate) remain)."""
+
+    def __init__(self, keys, re, im, gate):
+        self.keys, self.re, self.im, self.gate = keys, re, im, gate
+
+    def __len__(self):
+        return self.re.size
+
+
+def pauli_propagate_capture(gates, keys, re, im=None, capdeg=128, maxdegree=128, mincoeff=0.0, topk=0,
+                            max_xweight=-1, xtrunc_period=1, batched=True):
+    """Serial propagation that also returns the partners dropped by the degree
+    filter with degree in (maxdegree, capdeg]: (OraclePoly, Dropped)."""
+    L = lib()
+    gates = np.ascontiguousarray(gates, dtype=PAULI_GATE)
+    keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
+    re = np.ascontiguousarray(re, dtype=np.float64)
+    im = None if im is None else np.ascontiguousarray(im, dtype=np.float64)
+    p = _Params(int(maxdegree), int(topk), float(mincoeff), int(max_xweight),
+                int(xtrunc_period), int(bool(batched)), 1)
+    d = ctypes.c_void_p()
+    h = L.ffo_pauli_propagate_capture(_ptr(gates), gates.size, _ptr(keys), _ptr(re), _ptr(im),
+                                      re.size, ctypes.byref(p), int(capdeg), ctypes.byref(d))
+    if not h:
+        raise ValueError("oracle rejected the circuit")
+    m = L.ffo_drops_size(d)
+    dk = np.zeros((4, m), dtype=np.uint64)
+    dre, dim, dg = np.zeros(m), np.zeros(m), np.zeros(m, dtype=np.int64)
+    if m:
+        L.ffo_drops_copy(d, _ptr(dk), _ptr(dre), _ptr(dim), _ptr(dg))
+    L.ffo_drops_free(d)
+    return OraclePoly(h), Dropped(dk, dre, dim, dg)
 
 
 def majorana_propagate(gates, keys, re, im=None, maxdegree=None, mincoeff=0.0):
