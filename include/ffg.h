@@ -6,6 +6,8 @@
  * or a negative status, and ffg_last_error() gives the message.  One context
  * owns one CUDA stream on one device and must not be used from two threads at
  * once.  Device memory is pooled in the context and reused across calls.
+ * Results (ffg_result) and batches (ffg_batch) use their context's stream and
+ * scratch buffers: free them before destroying that context.
  *
  * Key layout (all entry points): uint64 arrays of shape [4][n] (plane-major).
  *   Pauli:    plane 0 = xory bits of qubits 0..63, plane 1 = xory of 64..127,
