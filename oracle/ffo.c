@@ -689,20 +689,15 @@ void ffo_drops_free(ffo_drops* d) {
 /* ------------------------------------------------------------------------- */
 
 /* merge_parity(term, gate): parity of #{(t, g) : t in term, g in gate, t < g}
- * (src/bits_utils.h:14-38), counted bit by bit as the reference does. */
+ * (src/bits_utils.h:14-38): for each set bit g of the gate, the term bits
+ * below it are counted. */
 static int merge_parity(const uint64_t* term, const uint64_t* gate) {
     int tot = 0;
-    for (int b = 255; b >= 0; b--) {
-        if (!((gate[b >> 6] >> (b & 63)) & 1ULL)) continue;
-        for (int w = 0; w < 4; w++) {
-            uint64_t below;
-            if (w < (b >> 6))
-                below = ~0ULL;
-            else if (w == (b >> 6))
-                below = (b & 63) ? ((1ULL << (b & 63)) - 1) : 0ULL;
-            else
-                below = 0ULL;
-            tot += popc(term[w] & below);
+    for (int wg = 0; wg < 4; wg++) {
+        for (uint64_t gb = gate[wg]; gb; gb &= gb - 1) {
+            const int b = __builtin_ctzll(gb);
+            for (int w = 0; w < wg; w++) tot += popc(term[w]);
+            tot += popc(term[wg] & ((1ULL << b) - 1));
         }
     }
     return tot & 1;
