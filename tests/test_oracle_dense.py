@@ -121,6 +121,15 @@ def test_pauli_oracle_equals_dense_heisenberg_product(seed):
     got = polynomial_matrix(r.keys, r.re, r.im, qubits)
     want = U.conj().T @ polynomial_matrix(keys, re, im, qubits) @ U
     np.testing.assert_allclose(got, want, rtol=0, atol=1e-12)
+    # expectations in computational basis states: <b|O|b>, qubit 0 leftmost
+    for _ in range(4):
+        bits = rng.integers(0, 2, size=n)
+        b = [0, 0]
+        for q, v in zip(qubits, bits):
+            b[q // 64] |= int(v) << (q % 64)
+        idx = int("".join(str(int(v)) for v in bits), 2)
+        assert abs(r.qubit_state(b[0], b[1]) - want[idx, idx]) <= 1e-12
+    assert abs(r.overlapwithzero() - want[0, 0]) <= 1e-12
 
 
 def gamma(n_modes, i):
@@ -172,3 +181,8 @@ def test_majorana_oracle_equals_dense_heisenberg_product(seed):
         obs += complex(re[t], im[t]) * majorana_matrix(keys[:, t], n_modes)
     want = U.conj().T @ obs @ U
     np.testing.assert_allclose(got, want, rtol=0, atol=1e-12)
+    # Fock states: <b|O|b> with mode pair j on qubit j
+    for occ in range(2 ** (n_modes // 2)):
+        bits = [(occ >> j) & 1 for j in range(n_modes // 2)]
+        idx = int("".join(str(v) for v in bits), 2)
+        assert abs(r.fock_state(occ, 0) - want[idx, idx]) <= 1e-12
