@@ -1,5 +1,6 @@
 """The oracle against dense linear algebra: without truncation, the propagated
-polynomial equals U^dagger O U.
+polynomial equals U^dagger O U; the Jordan-Wigner map and the sparse export give
+the same operators as their dense matrices.
 
 The reference's own circuit tests check propagation against the naive
 product U^dagger O U (pauli_circuit_test.py:53-92, majorana_circuit_test.py:6-41).
@@ -186,3 +187,39 @@ def test_majorana_oracle_equals_dense_heisenberg_product(seed):
         bits = [(occ >> j) & 1 for j in range(n_modes // 2)]
         idx = int("".join(str(v) for v in bits), 2)
         assert abs(r.fock_state(occ, 0) - want[idx, idx]) <= 1e-12
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_jordan_wigner_restatement_equals_dense_majorana_products(seed):
+    """jw maps every Majorana string to the Pauli string of the same operator."""
+    rng = np.random.default_rng(300 + seed)
+    n_modes = 8
+    keys = np.zeros((4, 6), dtype=np.uint64)
+    for t in range(6):
+        for i in rng.choice(n_modes, size=int(rng.integers(0, n_modes + 1)), replace=False):
+            keys[0, t] |= np.uint64(1) << np.uint64(int(i))
+    keys = np.unique(keys, axis=1)
+    re = rng.normal(size=keys.shape[1])
+    im = rng.normal(size=keys.shape[1])
+    pk, pre, pim = O.jordan_wigner(keys, re, im)
+    dim = 2 ** (n_modes // 2)
+    want = np.zeros((dim, dim), dtype=complex)
+    for t in range(keys.shape[1]):
+        want += complex(re[t], im[t]) * majorana_matrix(keys[:, t], n_modes)
+    got = polynomial_matrix(pk, pre, pim, list(range(n_modes // 2)))
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_sparse_restatement_equals_dense_matrix(seed):
+    """The CSC export is the dense matrix of the polynomial (qubit 0 leftmost)."""
+    from scipy.sparse import csc_matrix
+    rng = np.random.default_rng(400 + seed)
+    n = 4
+    keys = np.stack([random_pauli_key(rng, list(range(n)), int(rng.integers(1, n + 1))) for _ in range(8)], axis=1)
+    keys = np.unique(keys, axis=1)
+    re = rng.normal(size=keys.shape[1])
+    im = rng.normal(size=keys.shape[1])
+    indptr, indices, data = O.pauli_sparse(keys, re, im, n)
+    got = csc_matrix((data, indices, indptr), shape=(2 ** n, 2 ** n)).toarray()
+    np.testing.assert_allclose(got, polynomial_matrix(keys, re, im, list(range(n))), rtol=0, atol=1e-12)
