@@ -415,6 +415,15 @@ class FockState:
             j += 1
         return J
 
+    def vec(self, m, nocc=None):
+        """Dense basis vector of the state on m modes (mode 0 is the most
+        significant bit of the index, as in the sparse export)."""
+        if nocc is None:
+            v = [0.0] * (1 << m)
+            v[int(format(self.b, f"0{m}b")[::-1], 2) if m else 0] = 1.0
+            return v
+        raise NotImplementedError("subspace vectors are not provided")
+
     def __call__(self, o):
         if isinstance(o, MajoranaString):
             J = self._pairs(o.alpha)
