@@ -85,3 +85,31 @@ def test_identity_holds_through_clifford_segments():
     lab = _labels(tab, d, w2)
     assert abs(high.overlapwithzero() - low.overlapwithzero()) > 1e-3
     assert abs(high.overlapwithzero() - (low.overlapwithzero() + lab.sum())) <= 1e-12
+
+
+def _label_job(args):
+    tab, k, re, im, wmax, tau = args
+    return O.pauli_propagate(tab, k, re, im, maxdegree=wmax, mincoeff=tau).overlapwithzero()
+
+
+@pytest.mark.slow
+def test_labels_with_a_coefficient_threshold_kicked_ising_10x10():
+    """With the workload's threshold tau = 1e-6 the identity is approximate.
+    On the 10x10 kicked-Ising circuit (theta_h = 0.3), the W=6 value plus the
+    labels at W'=8 of the 909 dropped partners above tau comes within 1e-3 of
+    the W=8 value, although the two values differ by 0.28 (about 4 minutes on
+    8 cores)."""
+    from multiprocessing import get_context
+    tab = ff.encode_pauli_circuit(ff.build_circuit(ff.workloads.kicked_ising_circuit(0.3)))
+    k, re, im = _z(55)
+    tau = 1e-6
+    low, d = O.pauli_propagate_capture(tab, k, re, im, capdeg=8, maxdegree=6, mincoeff=tau)
+    high = O.pauli_propagate(tab, k, re, im, maxdegree=8, mincoeff=tau, n_threads=8)
+    sel = np.nonzero(np.hypot(d.re, d.im) > tau)[0]
+    jobs = [(tab[: int(d.gate[i])], d.keys[:, i : i + 1].copy(), d.re[i : i + 1].copy(), d.im[i : i + 1].copy(), 8,
+             tau) for i in sel]
+    with get_context("spawn").Pool(8) as pool:
+        lab = np.array(pool.map(_label_job, jobs, chunksize=4))
+    f_low, f_high = low.overlapwithzero(), high.overlapwithzero()
+    assert abs(f_high - f_low) > 0.2
+    assert abs(f_high - (f_low + lab.sum())) <= 1e-3
