@@ -1,14 +1,15 @@
 // Allocation-free Pauli rotation entry point (ffg_pauli_rotations_noalloc).
 //
 // Some callers cannot allocate device memory at the moment they need this
-// operation: code that runs while a CUDA stream is being captured (cudaMalloc
-// and cudaFree are not permitted under global capture mode), code that must
-// not cause the device-wide synchronisation that cudaFree implies (latency-
-// critical loops sharing the GPU with other streams), and processes in which a
-// framework already reserved the whole device memory pool for its own
-// allocator.  For them this file keeps the term store in one statically sized
-// device array, so the entry point creates no context and calls no cudaMalloc,
-// cudaMallocHost, cudaFree or any allocating library routine.
+// operation.  Two kinds are common: processes in which a framework's caching
+// allocator has already reserved (nearly) all device memory for itself, so a
+// cudaMalloc from a library fails or fragments that pool; and latency-critical
+// loops that share the GPU with other streams, where cudaFree's implicit
+// device-wide synchronisation is not acceptable.  For them this file keeps the
+// term store in one statically sized device array, so the entry point creates
+// no context and calls no cudaMalloc, cudaMallocHost, cudaFree or any
+// allocating library routine.  The caller still provides the input and output
+// arrays.
 //
 // Limits and sharing rules:
 //  * the scratch array holds at most kNoAllocCap = 65536 terms; inputs may have
@@ -21,8 +22,12 @@
 //    index slots, dead flags) itself.  Two calls whose GPU work overlaps (for
 //    example on two streams) race on the array and give wrong results;
 //  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture begins.
+//    (cudaGetSymbolAddress) with that device current and keeps it for the
+//    process; make that first call before any stream capture begins.  A
+//    cudaDeviceReset of that device invalidates the kept address: do not call
+//    this entry point on that device after a reset;
+//  * the call waits for its own work on `stream` to finish before it returns
+//    (it reads the result size and the error flags back to the host).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -104,8 +109,15 @@ int ffg_pauli_rotations_noalloc(void* stream, const uint64_t* keys_in, const dou
     cudaStream_t st = (cudaStream_t)stream;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    if (e != cudaSuccess)
         return fail(errbuf, errlen, FFG_ERR_CUDA, "ffg_pauli_rotations_noalloc: no current CUDA device");
+    if (dev < 0 || dev >= kMaxDevices) {
+        std::snprintf(msg, sizeof msg,
+                      "ffg_pauli_rotations_noalloc: device ordinal %d is beyond the %d devices this entry "
+                      "point supports",
+                      dev, kMaxDevices);
+        return fail(errbuf, errlen, FFG_ERR_ARG, msg);
+    }
     // once per device, with that device current: device address of the array
     {
         std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -178,10 +190,12 @@ int ffg_pauli_rotations_noalloc(void* stream, const uint64_t* keys_in, const dou
     if (h.error & 1u) return fail(errbuf, errlen, FFG_ERR_ARG, "ffg_pauli_rotations_noalloc: input contains duplicate keys");
     if (h.error) return fail(errbuf, errlen, FFG_ERR_STATE, "ffg_pauli_rotations_noalloc: index probe overrun");
     if (h.overflow) {
+        // h.overflow - 1 counts rotations in application order (last gate first)
+        const size_t applied = (size_t)(h.overflow - 1);
         std::snprintf(msg, sizeof msg,
                       "ffg_pauli_rotations_noalloc: the polynomial outgrew the fixed scratch limit "
-                      "of %llu terms at rotation %u",
-                      (unsigned long long)kNoAllocCap, h.overflow - 1);
+                      "of %llu terms at gates[%zu]",
+                      (unsigned long long)kNoAllocCap, ngates - 1 - applied);
         return fail(errbuf, errlen, FFG_ERR_ARG, msg);
     }
     *n_out = (size_t)h.n;

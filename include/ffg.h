@@ -254,11 +254,13 @@ void ffg_batch_free(ffg_batch* b);
 /* -------------------------------------------------------------------------- */
 /* Allocation-free rotations.  No counterpart in the reference: this entry
  * point exists for callers that cannot allocate device memory when they call
- * it (code running under stream capture, where cudaMalloc/cudaFree are not
- * permitted; loops that must not trigger the device-wide synchronisation of
- * cudaFree; processes whose device memory is reserved by another allocator).
- * It creates no context and calls no allocating CUDA or library routine: the
- * term store lives in a fixed 65536-term device array inside libffg.
+ * it -- processes in which a framework's caching allocator already holds
+ * (nearly) all device memory, so a library cudaMalloc fails or fragments that
+ * pool, and latency-critical loops that share the GPU with other streams and
+ * cannot accept cudaFree's implicit device-wide synchronisation.  It creates
+ * no context and calls no allocating CUDA or library routine: the term store
+ * lives in a fixed 65536-term device array inside libffg (about 4.3 MB, held
+ * by every GPU that loads the library until the process exits).
  *
  * Applies the FFG_ROT gates of gates[0..ngates) last to first, one reference
  * conjugation each (partners of weight > maxdegree are not emitted), with no
@@ -268,11 +270,14 @@ void ffg_batch_free(ffg_batch* b);
  * Work is issued on `stream` (a cudaStream_t; NULL = legacy default stream)
  * and the call returns after it completes.
  *   - n must be at most 32768 and the polynomial may not outgrow 65536 terms:
- *     larger sizes return FFG_ERR_ARG with a message in errbuf (may be NULL);
+ *     larger sizes return FFG_ERR_ARG with a message in errbuf (may be NULL)
+ *     naming the gates[] index at which it outgrew the array;
  *   - *n_out receives the result size even when out_cap is too small;
+ *   - duplicate input keys return FFG_ERR_ARG;
  *   - the first call on a device looks up the device address of the array
- *     (once per device, with that device current); make it before any stream
- *     capture begins;
+ *     (once per device, with that device current) and keeps it; make that
+ *     first call before any stream capture begins.  A cudaDeviceReset of the
+ *     device invalidates the kept address;
  *   - all calls share the one array and each leaves its contents behind; calls
  *     whose GPU work overlaps (e.g. on two streams) race and give wrong results.
  */

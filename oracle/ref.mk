@@ -6,7 +6,7 @@
 #
 # The reference tree is only available in the development container; on
 # machines without it this recipe is skipped by the build helper.
-REF      ?= /root/reference
+REF      ?= $(or $(FFG_REFERENCE_SRC),/root/reference)
 PYTHON   ?= python3
 OUT      := oracle/_ref
 EXT      := $(shell $(PYTHON) -c "import sysconfig;print(sysconfig.get_config_var('EXT_SUFFIX'))")

@@ -454,7 +454,7 @@ def transform_cases(ff):
     yield "sparse_dropped_qubits", lambda: sparse_case("sparse_dropped_qubits", random_pauli_poly(ff, rng, list(range(7)), 25, True, 3), 5)
 
 
-REF = "/root/reference"
+REF = os.environ.get("FFG_REFERENCE_SRC", "/root/reference")
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
