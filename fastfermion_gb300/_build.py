@@ -6,7 +6,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libffg.so")
-SOURCES = ["ffg_engine.cu", "ffg_noalloc.cu", "ffg_sortmerge.cu"]
+SOURCES = ["ffg_engine.cu", "ffg_noalloc.cu", "ffg_sortmerge.cu", "ffg_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -58,7 +58,12 @@ EXPORTS = ["ffg_create", "ffg_destroy", "ffg_last_error", "ffg_set_profiling", "
            "ffg_pauli_schedule", "ffg_stream", "ffg_pauli_rotations_noalloc",
            "ffg_pauli_propagate_batched", "ffg_batch_size", "ffg_batch_copy", "ffg_batch_adjoint",
            "ffg_batch_free", "ffg_majorana_to_pauli", "ffg_result_sparse", "ffg_set_option",
-           "ffg_get_option"]
+           "ffg_get_option", "ffg_pauli_propagate_instances", "ffg_pauli_propagate_capture", "ffg_drops_size",
+           "ffg_drops_copy", "ffg_drops_device", "ffg_drops_free", "ffg_mlp_create", "ffg_mlp_free",
+           "ffg_mlp_last_error", "ffg_mlp_set_params", "ffg_mlp_get_params", "ffg_mlp_forward", "ffg_mlp_gradient",
+           "ffg_mlp_adam_step", "ffg_mlp_correction", "ffg_mlp_selftest_gemm", "ffg_drop_features"]
+
+MLP_IN, MLP_HIDDEN, MLP_NPARAMS = 32, 128, 37377
 
 
 def lib():
@@ -100,6 +105,31 @@ def lib():
                                                       ctypes.c_char_p, sz]
             L.ffg_pauli_propagate_batched.argtypes = [vp, vp, vp, sz, vp, sz, ctypes.POINTER(PauliParams),
                                                       ctypes.POINTER(BatchParams), vp, ctypes.POINTER(vp)]
+            L.ffg_pauli_propagate_instances.argtypes = [vp, vp, vp, sz, vp, sz, ctypes.POINTER(PauliParams),
+                                                        ctypes.POINTER(BatchParams), vp, vp, ctypes.POINTER(vp)]
+            L.ffg_pauli_propagate_capture.argtypes = [vp, vp, vp, vp, sz, vp, sz, ctypes.POINTER(PauliParams),
+                                                      ctypes.c_int, ctypes.c_int32, ctypes.c_double,
+                                                      ctypes.POINTER(vp), ctypes.POINTER(vp)]
+            L.ffg_drops_size.restype = sz
+            L.ffg_drops_size.argtypes = [vp]
+            L.ffg_drops_copy.argtypes = [vp, vp, vp, vp, vp]
+            L.ffg_drops_device.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(sz), ctypes.POINTER(vp),
+                                           ctypes.POINTER(vp), ctypes.POINTER(vp)]
+            L.ffg_drops_free.argtypes = [vp]
+            L.ffg_mlp_create.argtypes = [vp, ctypes.POINTER(vp)]
+            L.ffg_mlp_free.argtypes = [vp]
+            L.ffg_mlp_last_error.restype = ctypes.c_char_p
+            L.ffg_mlp_last_error.argtypes = [vp]
+            L.ffg_mlp_set_params.argtypes = [vp, vp]
+            L.ffg_mlp_get_params.argtypes = [vp, vp]
+            L.ffg_mlp_forward.argtypes = [vp, vp, sz, vp]
+            L.ffg_mlp_gradient.argtypes = [vp, vp, vp, vp, sz, vp, dp]
+            L.ffg_mlp_adam_step.argtypes = [vp, vp, vp, vp, sz, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                            ctypes.c_float, dp]
+            L.ffg_mlp_correction.argtypes = [vp, vp, vp, sz, vp, dp]
+            L.ffg_mlp_selftest_gemm.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp]
+            L.ffg_drop_features.argtypes = [vp, vp, sz, vp, vp, sz, vp, sz, vp, ctypes.c_int32, vp, ctypes.c_int32,
+                                            ctypes.c_int32, vp, vp]
             L.ffg_batch_size.restype = sz
             L.ffg_batch_size.argtypes = [vp]
             L.ffg_batch_copy.argtypes = [vp, vp, vp, vp]
@@ -145,7 +175,7 @@ class Context:
 
     OPTIONS = ("orbit_route_big", "orbit_team", "orbit_window", "orbit_min_gates", "orbit_qidx", "pdl",
                "morbit", "morbit_min_gates", "morbit_route_big", "merge_sort", "orbit_team_threads",
-               "orbit_block_threads")
+               "orbit_block_threads", "min_capacity", "store_headroom", "group_region_cap")
 
     def set_option(self, name, value):
         self.check(self.L.ffg_set_option(self.h, name.encode(), int(value)))
@@ -223,6 +253,50 @@ class Context:
                                                       _ptr(expect), ctypes.byref(out)))
         return expect, Batch(self, out, ninst, int(np.sum(gates["kind"] == ROT)), re.size)
 
+    def pauli_propagate_instances(self, keys, re, offsets, gates, thetas, params, active=None):
+        """ffg_pauli_propagate_instances: as pauli_propagate_batched (no adjoint) with
+        per-instance active rotations: active is None or uint64 (ninst, W), W =
+        max(1, ceil(nrot / 64)), bit r set = rotation r acts on the instance.
+        Returns (expect[ninst], Batch)."""
+        keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
+        re = np.ascontiguousarray(re, dtype=np.float64)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        gates = np.ascontiguousarray(gates, dtype=PAULI_GATE)
+        ninst = offsets.size - 1
+        nrot = int(np.sum(gates["kind"] == ROT))
+        th = None if thetas is None else np.ascontiguousarray(thetas, dtype=np.float64)
+        act = None
+        if active is not None:
+            act = np.ascontiguousarray(active, dtype=np.uint64).reshape(ninst, -1)
+            if act.shape[1] != max(1, (nrot + 63) // 64):
+                raise ValueError("active must have max(1, ceil(nrot / 64)) words per instance")
+        bp = BatchParams(ninst, offsets.ctypes.data, th.ctypes.data if th is not None and th.size else None, 0, 0)
+        p = PauliParams(**params)
+        expect = np.zeros(ninst)
+        out = ctypes.c_void_p()
+        self.check(self.L.ffg_pauli_propagate_instances(self.h, _ptr(keys), _ptr(re), re.size, _ptr(gates),
+                                                        gates.size, ctypes.byref(p), ctypes.byref(bp), _ptr(act),
+                                                        _ptr(expect), ctypes.byref(out)))
+        return expect, Batch(self, out, ninst, nrot, re.size)
+
+    def pauli_propagate_capture(self, keys, re, im, gates, params, capdeg, min_abs=0.0, on_device=False):
+        """ffg_pauli_propagate_capture: (Result, Drops) -- the propagation and the
+        partners the degree filter dropped (degree <= capdeg, |value| > min_abs)."""
+        out, dr = ctypes.c_void_p(), ctypes.c_void_p()
+        if on_device:
+            kp, rp, ip, n = keys, re, im, params.pop("n")
+        else:
+            keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
+            re = np.ascontiguousarray(re, dtype=np.float64)
+            im = None if im is None else np.ascontiguousarray(im, dtype=np.float64)
+            kp, rp, ip, n = _ptr(keys), _ptr(re), _ptr(im), re.size
+        gates = np.ascontiguousarray(gates, dtype=PAULI_GATE)
+        p = PauliParams(**params)
+        self.check(self.L.ffg_pauli_propagate_capture(self.h, kp, rp, ip, n, _ptr(gates), gates.size,
+                                                      ctypes.byref(p), int(bool(on_device)), int(capdeg),
+                                                      float(min_abs), ctypes.byref(out), ctypes.byref(dr)))
+        return Result(self, out), Drops(self, dr)
+
     def majorana_to_pauli(self, keys, re, im):
         """Jordan-Wigner map of Majorana terms (host arrays) to a Pauli Result."""
         keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
@@ -266,6 +340,136 @@ class Batch:
     def free(self):
         if self.h is not None and self.h.value:
             self.ctx.L.ffg_batch_free(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _dptr(t):
+    """device address of a torch tensor (or an integer address, or None)"""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return ctypes.c_void_p(t)
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class MLP:
+    """The surrogate network of the learned correction (ffg_mlp), on a context's
+    stream.  Device arrays are torch CUDA tensors (or integer addresses): x BF16
+    (torch.bfloat16 or int16 bit patterns) [n][32], target/weight/y FP32 [n]."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.L = ctx.L
+        self.h = ctypes.c_void_p()
+        ctx.check(self.L.ffg_mlp_create(ctx.h, ctypes.byref(self.h)))
+
+    def check(self, rc):
+        if rc != 0:
+            msg = self.L.ffg_mlp_last_error(self.h).decode()
+            if rc == -1:
+                raise RuntimeError(msg)
+            raise FFGError(f"libffg MLP error {rc}: {msg}")
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == MLP_NPARAMS
+        self.check(self.L.ffg_mlp_set_params(self.h, _ptr(p)))
+
+    def get_params(self):
+        p = np.zeros(MLP_NPARAMS, dtype=np.float32)
+        self.check(self.L.ffg_mlp_get_params(self.h, _ptr(p)))
+        return p
+
+    def forward(self, x, n, y):
+        self.check(self.L.ffg_mlp_forward(self.h, _dptr(x), int(n), _dptr(y)))
+
+    def gradient(self, x, target, weight, n):
+        """(grad (NPARAMS,) float32, loss)"""
+        g = np.zeros(MLP_NPARAMS, dtype=np.float32)
+        loss = ctypes.c_double()
+        self.check(self.L.ffg_mlp_gradient(self.h, _dptr(x), _dptr(target), _dptr(weight), int(n), _ptr(g),
+                                           ctypes.byref(loss)))
+        return g, loss.value
+
+    def adam_step(self, x, target, weight, n, lr, beta1=0.9, beta2=0.999, eps=1e-8, want_loss=False):
+        loss = ctypes.c_double()
+        self.check(self.L.ffg_mlp_adam_step(self.h, _dptr(x), _dptr(target), _dptr(weight), int(n), float(lr),
+                                            float(beta1), float(beta2), float(eps),
+                                            ctypes.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+    def correction(self, x, coef, n, t):
+        out = ctypes.c_double()
+        self.check(self.L.ffg_mlp_correction(self.h, _dptr(x), _dptr(coef), int(n), _dptr(t), ctypes.byref(out)))
+        return out.value
+
+    def selftest_gemm(self, a_bits, b_bits):
+        """D = A B^T for host BF16 bit patterns A (128, K), B (N, K) -> (128, N)"""
+        a = np.ascontiguousarray(a_bits, dtype=np.uint16)
+        b = np.ascontiguousarray(b_bits, dtype=np.uint16)
+        n, k = b.shape
+        d = np.zeros((128, n), dtype=np.float32)
+        self.check(self.L.ffg_mlp_selftest_gemm(self.h, int(n), int(k), _ptr(a), _ptr(b), _ptr(d)))
+        return d
+
+    def free(self):
+        if self.h is not None and self.h.value:
+            self.L.ffg_mlp_free(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def drop_features(ctx, keys, stride, coef, gate, n, gates, batch_of_gate, nbatches, coords, obs, maxdegree,
+                  feat=None, x=None):
+    """ffg_drop_features on device arrays (torch tensors or addresses)."""
+    gates = np.ascontiguousarray(gates, dtype=PAULI_GATE)
+    bog = np.ascontiguousarray(batch_of_gate, dtype=np.int32)
+    co = np.ascontiguousarray(coords, dtype=np.float32).reshape(2, 128)
+    ctx.check(ctx.L.ffg_drop_features(ctx.h, _dptr(keys), int(stride), _dptr(coef), _dptr(gate), int(n),
+                                      _ptr(gates), gates.size, _ptr(bog), int(nbatches), _ptr(co), int(obs),
+                                      int(maxdegree), _dptr(feat), _dptr(x)))
+
+
+class Drops:
+    """Partners dropped by the degree filter (ffg_drops), held in device memory."""
+
+    def __init__(self, ctx, handle):
+        self.ctx, self.h = ctx, handle
+        self.n = ctx.L.ffg_drops_size(handle)
+
+    def __len__(self):
+        return self.n
+
+    def copy(self):
+        """(keys (4, n), re, im, gate) sorted by gate, then key."""
+        keys = np.zeros((4, self.n), dtype=np.uint64)
+        re, im = np.zeros(self.n), np.zeros(self.n)
+        gate = np.zeros(self.n, dtype=np.int32)
+        if self.n:
+            self.ctx.check(self.ctx.L.ffg_drops_copy(self.h, _ptr(keys), _ptr(re), _ptr(im), _ptr(gate)))
+        return keys, re, im, gate
+
+    def device(self):
+        """(keys, stride, re, im, gate) device addresses."""
+        k, st, r, i, g = ctypes.c_void_p(), ctypes.c_size_t(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        self.ctx.check(self.ctx.L.ffg_drops_device(self.h, ctypes.byref(k), ctypes.byref(st), ctypes.byref(r),
+                                                   ctypes.byref(i), ctypes.byref(g)))
+        return k.value, st.value, r.value, i.value, g.value
+
+    def free(self):
+        if self.h is not None and self.h.value:
+            self.ctx.L.ffg_drops_free(self.h)
         self.h = None
 
     def __del__(self):

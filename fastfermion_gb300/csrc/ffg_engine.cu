@@ -141,6 +141,9 @@ struct BatchCtx {
     int inst_plane = 0;                  // store plane of the instance code
     int inst_shift = 0;
     u64 inst_mask = 0;
+    const u64* d_active = nullptr;       // [ninst][active_words] active rotations (null: all)
+    u32 active_words = 0;
+    u32 nrot = 0;                        // rotations of the circuit (batch gate b = rotation nrot-1-b)
 };
 
 }  // namespace
@@ -188,6 +191,11 @@ struct ffg_ctx {
     void* d_smscratch = nullptr;
     size_t smscratch_bytes = 0;
     int morbit_min_gates = 2;   // shortest Majorana run sent to the batch-orbit path
+    u64 min_capacity = 1ull << 16;      // smallest term-store capacity (option min_capacity)
+    int store_headroom = 4;             // orbit windows size their stores for this many times
+                                        // the entering terms (option store_headroom)
+    u64 group_region_cap = 1ull << 14;  // members of a first global-memory group region (Pauli;
+                                        // Majorana starts at a quarter of it)
     int morbit_route_big = 12;  // |A| from which a Majorana group skips the warp tier (FFG_MORBIT_ROUTE);
                                 // 6x6 Hubbard: 323 ms at 12 or 16, 329 ms at 10, 356 ms at 8
     MBatchGate* d_mgates = nullptr;
@@ -204,6 +212,8 @@ struct ffg_ctx {
     OrbitCounters* h_ocw = nullptr;  // pinned
     RawBuf bigpool;                 // global-memory tables of large orbit groups
     const BatchCtx* batch = nullptr;  // set while a batched propagation runs
+    CaptureArgs capture{};            // set while a capture propagation runs (n null: off)
+    RawBuf capbuf;                    // capture records and their index
     ffg_profile prof{};
     std::vector<PendingEvent> events;
     std::vector<cudaEvent_t> free_events;
@@ -231,6 +241,7 @@ struct ffg_batch {
     size_t ninst = 0, nrot = 0, n_input = 0;
     BatchCtx bc{};
     double2* d_inst_cs = nullptr;
+    u64* d_active = nullptr;         // per-instance active rotations (null: all)
     u64 xmask[2] = {0, 0};           // qubit bits of the x planes (caller words 0, 1)
     int inst_word = 0;               // caller word that holds the instance code
     int maxdeg = 128;                // degree filter including the instance bits
@@ -396,6 +407,9 @@ struct Engine {
     int active = 0;  // which RawBuf holds the live store
     Store cur;
     u64 cap = 0;
+    // circuit gate index of every group (one rotation per group), for the
+    // capture records; null when not needed
+    const std::vector<int>* group_gate = nullptr;
 
     explicit Engine(ffg_ctx* c) : ctx(c) {}
 
@@ -443,7 +457,7 @@ struct Engine {
     int load(const uint64_t* keys, const double* re, const double* im, size_t n, int on_device,
              int pauli_nw_in /* planes layout of the caller: 4 planes */) {
         (void)pauli_nw_in;
-        cap = pow2_at_least(std::max<u64>((u64)n * 4, 1u << 16));
+        cap = pow2_at_least(std::max<u64>((u64)n * 4, ctx->min_capacity));
         int rc = ensure_buf(ctx, ctx->buf[0], store_bytes(KW, CPLX, cap));
         if (rc) return rc;
         active = 0;
@@ -921,7 +935,7 @@ struct Engine {
         constexpr int NWo = PAULI ? NW : 1;
         u32* list = ctx->orbit_team ? sc.big : retry_list;
         u32* other = ctx->orbit_team ? retry_list : sc.big;
-        u64 rcap = 1ull << 14;
+        u64 rcap = ctx->group_region_cap;
         while (nleft > 0) {
             const u32 grid = std::min<u32>(nleft, (u32)ctx->num_sms);
             BigPool bp{};
@@ -1027,7 +1041,13 @@ struct Engine {
             a.inst_plane = ctx->batch->inst_plane;
             a.inst_shift = ctx->batch->inst_shift;
             a.inst_mask = ctx->batch->inst_mask;
+            if (ctx->batch->d_active) {
+                a.active = ctx->batch->d_active;
+                a.active_words = ctx->batch->active_words;
+                a.act_r0 = (int)ctx->batch->nrot - 1 - j.g0;
+            }
         }
+        a.cap = ctx->capture;
         return a;
     }
 
@@ -1071,7 +1091,8 @@ struct Engine {
         while (i < njobs) {
             const u64 n_cur = ctx->h_ctr->n;  // dense store: no dead entries
             if (n_cur == 0) return FFG_OK;  // every later batch is empty too
-            const u64 wcap = std::max<u64>(std::max<u64>(cap, pow2_at_least(4 * n_cur)), grow);
+            const u64 wcap =
+                std::max<u64>(std::max<u64>(cap, pow2_at_least((u64)ctx->store_headroom * n_cur)), grow);
             int rc = FFG_OK;
             if (cap < wcap) {
                 rc = compact_into(1 - active, wcap);
@@ -1399,7 +1420,7 @@ struct Engine {
             bool overflow = (ctx->h_oc->overflow & 1u) != 0;
             u32* list = retry_list;
             u32* other = sc.big;
-            u32 rcap = 4096;
+            u32 rcap = (u32)std::max<u64>(ctx->group_region_cap / 4, 64);
             while (!overflow && nleft > 0) {
                 if (rcap > (1u << 22)) return set_err(ctx, FFG_ERR_STATE, "Majorana orbit group larger than 2^22 terms");
                 const u32 grid = std::min<u32>(nleft, (u32)ctx->num_sms);
@@ -1516,6 +1537,7 @@ struct Engine {
             b.c = ga.c[0];
             b.s = ga.s[0];
             b.yP = ga.yP[0];
+            b.gidx = group_gate && ops[o].idx < (int)group_gate->size() ? (*group_gate)[ops[o].idx] : -1;
             gate_of_op[o] = (int)bg.size();
             bg.push_back(b);
         }
@@ -1620,7 +1642,7 @@ struct Engine {
     // Loads a checkpoint (store planes, dense) as the live store.
     int restore(const AdjRecord& r) {
         const u64 n = r.n_in;
-        cap = pow2_at_least(std::max<u64>((u64)n * 4, 1u << 16));
+        cap = pow2_at_least(std::max<u64>((u64)n * 4, ctx->min_capacity));
         int rc = ensure_buf(ctx, ctx->buf[0], store_bytes(KW, CPLX, cap));
         if (rc) return rc;
         active = 0;
@@ -1820,7 +1842,10 @@ void add_groups(const ffg_pauli_gate* g, const std::vector<size_t>& run, const f
 void build_pauli_ops(const ffg_pauli_gate* g, size_t ng, const ffg_pauli_params& p, int nw,
                      std::vector<Op>& ops, std::vector<RotArgs>& rots, std::vector<TruncArgs>& truncs,
                      std::vector<int64_t>* batches, std::vector<GArgs>* groups = nullptr,
-                     int dmax = kGroupD, std::vector<BatchInfo>* binfo = nullptr) {
+                     int dmax = kGroupD, std::vector<BatchInfo>* binfo = nullptr,
+                     std::vector<int>* rot_gates = nullptr) {
+    // rot_gates: circuit index of every rotation in application order (with
+    // dmax = 1 its position is the index of the rotation's group)
     int rot_count = 0;
     auto add_rot = [&](size_t i) {
         RotArgs a{};
@@ -1870,6 +1895,7 @@ void build_pauli_ops(const ffg_pauli_gate* g, size_t ng, const ffg_pauli_params&
                     add_groups(g, std::vector<size_t>{(size_t)i}, p, nw, dmax, ops, *groups);
                 else
                     add_rot((size_t)i);
+                if (rot_gates) rot_gates->push_back((int)i);
                 const int nrot = (int)ops.size() - first;
                 if (batches) batches->push_back(1);
                 const size_t before = ops.size();
@@ -1897,6 +1923,8 @@ void build_pauli_ops(const ffg_pauli_gate* g, size_t ng, const ffg_pauli_params&
                                ops, *groups);
                 else
                     for (size_t t = s; t < e; t++) add_rot(buf[t]);
+                if (rot_gates)
+                    for (size_t t = s; t < e; t++) rot_gates->push_back((int)buf[t]);
                 const int nrot = (int)ops.size() - first;
                 if (batches) batches->push_back((int64_t)(e - s));
                 rot_count += (int)(e - s);
@@ -1943,8 +1971,10 @@ int run_engine(ffg_ctx* ctx, const uint64_t* keys, const double* re, const doubl
                int on_device, const std::vector<Op>& ops, const std::vector<RotArgs>& rots,
                const std::vector<TruncArgs>& truncs, const std::vector<GArgs>& groups,
                bool deterministic, ffg_result** out, const std::vector<BatchInfo>* binfo = nullptr,
-               int maxdeg = 128, const std::vector<std::pair<int, int>>* mruns = nullptr) {
+               int maxdeg = 128, const std::vector<std::pair<int, int>>* mruns = nullptr,
+               const std::vector<int>* rot_gates = nullptr) {
     Engine<KW, CPLX, PAULI> E(ctx);
+    E.group_gate = rot_gates;
     int rc = E.load(keys, re, im, n, on_device, 0);
     if (rc) return rc;
     bool has_topk = false;
@@ -2347,6 +2377,7 @@ int ffg_destroy(ffg_ctx* ctx) {
     if (ctx->d_smscratch) cudaFree(ctx->d_smscratch);
     if (ctx->d_oscratch) cudaFree(ctx->d_oscratch);
     if (ctx->bigpool.p) cudaFree(ctx->bigpool.p);
+    if (ctx->capbuf.p) cudaFree(ctx->capbuf.p);
     if (ctx->d_oc) cudaFree(ctx->d_oc);
     if (ctx->h_oc) cudaFreeHost(ctx->h_oc);
     if (ctx->d_ocw) cudaFree(ctx->d_ocw);
@@ -2375,11 +2406,13 @@ int ffg_profile_get(const ffg_ctx* ctx, ffg_profile* out) {
 
 void* ffg_stream(const ffg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
-int ffg_pauli_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im,
-                        size_t n, const ffg_pauli_gate* gates, size_t ngates,
-                        const ffg_pauli_params* params, int on_device, ffg_result** out) {
-    if (!ctx || !out || !params || (n && (!keys || !re)) || (ngates && !gates)) return FFG_ERR_ARG;
-    *out = nullptr;
+namespace {
+// Body of ffg_pauli_propagate; with `capture` the orbit kernels also record
+// the partners the degree filter drops (ctx->capture is set by the caller)
+// and every commuting run goes through the orbit path.
+int pauli_propagate_impl(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im,
+                         size_t n, const ffg_pauli_gate* gates, size_t ngates,
+                         const ffg_pauli_params* params, int on_device, ffg_result** out, bool capture) {
     try {
         auto t0 = std::chrono::steady_clock::now();
         reset_profile(ctx);
@@ -2428,31 +2461,216 @@ int ffg_pauli_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, co
         std::vector<TruncArgs> truncs;
         std::vector<GArgs> groups;
         std::vector<BatchInfo> binfo;
+        std::vector<int> rot_gates;
         build_pauli_ops(gates, ngates, *params, nw, ops, rots, truncs, nullptr, &groups, ctx->group_d,
-                        &binfo);
+                        &binfo, capture ? &rot_gates : nullptr);
         int64_t nrot = 0;
         for (const auto& gr : groups) nrot += gr.ng;
         ctx->prof.n_gates = nrot;
         int rc = upload_cliffords(ctx, gates, ngates);
         if (rc) return rc;
         const bool det = params->deterministic != 0;
+        const std::vector<int>* rg = capture ? &rot_gates : nullptr;
+        const int min_gates = ctx->orbit_min_gates;
+        if (capture) ctx->orbit_min_gates = 1;  // every run through the orbit kernels (they record)
         if (nw == 1 && !cplx)
             rc = run_engine<2, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out,
-                                                &binfo, params->maxdegree);
+                                                &binfo, params->maxdegree, nullptr, rg);
         else if (nw == 1)
             rc = run_engine<2, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out,
-                                                &binfo, params->maxdegree);
+                                                &binfo, params->maxdegree, nullptr, rg);
         else if (!cplx)
             rc = run_engine<4, false, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out,
-                                                &binfo, params->maxdegree);
+                                                &binfo, params->maxdegree, nullptr, rg);
         else
             rc = run_engine<4, true, true>(ctx, keys, re, im, n, on_device, ops, rots, truncs, groups, det, out,
-                                                &binfo, params->maxdegree);
+                                                &binfo, params->maxdegree, nullptr, rg);
+        ctx->orbit_min_gates = min_gates;
         ctx->prof.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return rc;
     } catch (const std::exception& ex) {
         return set_err(ctx, FFG_ERR_STATE, ex.what());
     }
+}
+
+// keeps the capture records that are not repeats (gate >= 0), in any order
+__global__ void capture_compact(CaptureArgs cp, u64 n, u64* key, double* re, double* im, int32_t* gate,
+                                size_t stride, unsigned long long* cnt) {
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+        const int g = cp.gate[i];
+        if (g < 0) continue;
+        const u64 j = atomicAdd(cnt, 1ull);
+        for (int w = 0; w < 4; w++) key[w * stride + j] = cp.key[(u64)w * cp.cap + i];
+        re[j] = cp.re[i];
+        im[j] = cp.im[i];
+        gate[j] = g;
+    }
+}
+}  // namespace
+
+struct ffg_drops {
+    int device = 0;
+    size_t n = 0;
+    u64* key = nullptr;     // [4][n] caller layout
+    double* re = nullptr;
+    double* im = nullptr;
+    int32_t* gate = nullptr;
+};
+
+int ffg_pauli_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im,
+                        size_t n, const ffg_pauli_gate* gates, size_t ngates,
+                        const ffg_pauli_params* params, int on_device, ffg_result** out) {
+    if (!ctx || !out || !params || (n && (!keys || !re)) || (ngates && !gates)) return FFG_ERR_ARG;
+    *out = nullptr;
+    return pauli_propagate_impl(ctx, keys, re, im, n, gates, ngates, params, on_device, out, false);
+}
+
+void ffg_drops_free(ffg_drops* d) {
+    if (!d) return;
+    cudaSetDevice(d->device);
+    if (d->key) cudaFree(d->key);
+    if (d->re) cudaFree(d->re);
+    if (d->im) cudaFree(d->im);
+    if (d->gate) cudaFree(d->gate);
+    delete d;
+}
+
+int ffg_pauli_propagate_capture(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im,
+                                size_t n, const ffg_pauli_gate* gates, size_t ngates,
+                                const ffg_pauli_params* params, int on_device, int32_t capdeg, double min_abs,
+                                ffg_result** out, ffg_drops** drops) {
+    if (!ctx || !out || !drops || !params || (n && (!keys || !re)) || (ngates && !gates)) return FFG_ERR_ARG;
+    *out = nullptr;
+    *drops = nullptr;
+    if (!params->batched || params->topk > 0)
+        return set_err(ctx, FFG_ERR_ARG, "capture needs batched mode without top-k truncation");
+    if (!(min_abs >= 0.0)) return set_err(ctx, FFG_ERR_ARG, "capture: min_abs must be >= 0");
+    if (ctx->merge_sort || !ctx->orbit || !ctx->persistent || ctx->group_d != 1)
+        return set_err(ctx, FFG_ERR_ARG, "capture needs the orbit path (merge_sort off, no FFG_* overrides)");
+    if (capdeg <= params->maxdegree) return set_err(ctx, FFG_ERR_ARG, "capture: capdeg must exceed maxdegree");
+    try {
+        CK(cudaSetDevice(ctx->device));
+        u64 cap = 1ull << 16;
+        for (int attempt = 0; attempt < 8; attempt++) {
+            const size_t need = align256(4 * cap * 8) + 2 * align256(cap * 8) + align256(cap * 4) +
+                                align256(2 * cap * 4) + 256;
+            int rc = ensure_buf(ctx, ctx->capbuf, need);
+            if (rc) return rc;
+            char* p = ctx->capbuf.p;
+            CaptureArgs cp{};
+            cp.key = (u64*)p;
+            p += align256(4 * cap * 8);
+            cp.re = (double*)p;
+            p += align256(cap * 8);
+            cp.im = (double*)p;
+            p += align256(cap * 8);
+            cp.gate = (int*)p;
+            p += align256(cap * 4);
+            cp.slot = (u32*)p;
+            p += align256(2 * cap * 4);
+            cp.n = (u64*)p;
+            cp.cap = cap;
+            cp.maxdeg = capdeg;
+            cp.min_abs = min_abs;
+            CK(cudaMemsetAsync(cp.slot, 0, 2 * cap * 4 + 256, ctx->stream));  // index and counter
+            ctx->capture = cp;
+            ffg_result* r = nullptr;
+            rc = pauli_propagate_impl(ctx, keys, re, im, n, gates, ngates, params, on_device, &r, true);
+            ctx->capture = CaptureArgs{};
+            if (rc) return rc;
+            u64 claimed = 0;
+            CK(cudaMemcpyAsync(&claimed, cp.n, 8, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            if (claimed > cap) {  // too small: run again with room for every record
+                ffg_result_free(r);
+                cap = pow2_at_least(2 * claimed);
+                continue;
+            }
+            auto* d = new ffg_drops();
+            std::unique_ptr<ffg_drops, void (*)(ffg_drops*)> guard(d, ffg_drops_free);
+            d->device = ctx->device;
+            const size_t m = std::max<u64>(claimed, 1);
+            CK(cudaMalloc(&d->key, 4 * m * 8));
+            CK(cudaMalloc(&d->re, m * 8));
+            CK(cudaMalloc(&d->im, m * 8));
+            CK(cudaMalloc(&d->gate, m * 4));
+            unsigned long long* cnt = (unsigned long long*)cp.n;  // reused as the compaction counter
+            CK(cudaMemsetAsync(cnt, 0, 8, ctx->stream));
+            if (claimed) {
+                capture_compact<<<grid_for(ctx, claimed), kBlock, 0, ctx->stream>>>(cp, claimed, d->key, d->re, d->im,
+                                                                                   d->gate, m, cnt);
+                CK(cudaGetLastError());
+            }
+            u64 kept = 0;
+            CK(cudaMemcpyAsync(&kept, cnt, 8, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            d->n = kept;
+            // key planes were written with stride m; keep that stride as the
+            // capacity and report kept entries
+            if (kept != m && kept) {
+                // repack the planes to stride kept
+                u64* k2 = nullptr;
+                CK(cudaMalloc(&k2, 4 * kept * 8));
+                for (int w = 0; w < 4; w++)
+                    CK(cudaMemcpyAsync(k2 + (size_t)w * kept, d->key + (size_t)w * m, kept * 8,
+                                       cudaMemcpyDeviceToDevice, ctx->stream));
+                CK(cudaStreamSynchronize(ctx->stream));
+                cudaFree(d->key);
+                d->key = k2;
+            }
+            *out = r;
+            *drops = guard.release();
+            return FFG_OK;
+        }
+        return set_err(ctx, FFG_ERR_STATE, "capture: record buffer kept overflowing");
+    } catch (const std::exception& ex) {
+        return set_err(ctx, FFG_ERR_STATE, ex.what());
+    }
+}
+
+size_t ffg_drops_size(const ffg_drops* d) { return d ? d->n : 0; }
+
+int ffg_drops_device(const ffg_drops* d, const uint64_t** keys, size_t* stride, const double** re,
+                     const double** im, const int32_t** gate) {
+    if (!d) return FFG_ERR_ARG;
+    if (keys) *keys = (const uint64_t*)d->key;
+    if (stride) *stride = d->n;
+    if (re) *re = d->re;
+    if (im) *im = d->im;
+    if (gate) *gate = d->gate;
+    return FFG_OK;
+}
+
+int ffg_drops_copy(const ffg_drops* d, uint64_t* keys, double* re, double* im, int32_t* gate) {
+    if (!d || (d->n && (!keys || !re))) return FFG_ERR_ARG;
+    const size_t n = d->n;
+    if (!n) return FFG_OK;
+    if (cudaSetDevice(d->device) != cudaSuccess) return FFG_ERR_CUDA;
+    std::vector<u64> k(4 * n);
+    std::vector<double> r(n), i(n);
+    std::vector<int32_t> g(n);
+    if (cudaMemcpy(k.data(), d->key, 4 * n * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(r.data(), d->re, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(i.data(), d->im, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(g.data(), d->gate, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return FFG_ERR_CUDA;
+    // deterministic order: by gate, then key words 0..3
+    std::vector<size_t> ord(n);
+    for (size_t t = 0; t < n; t++) ord[t] = t;
+    std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
+        if (g[a] != g[b]) return g[a] < g[b];
+        for (int w = 0; w < 4; w++)
+            if (k[w * n + a] != k[w * n + b]) return k[w * n + a] < k[w * n + b];
+        return false;
+    });
+    for (size_t t = 0; t < n; t++) {
+        const size_t s = ord[t];
+        for (int w = 0; w < 4; w++) keys[w * n + t] = k[w * n + s];
+        re[t] = r[s];
+        if (im) im[t] = i[s];
+        if (gate) gate[t] = g[s];
+    }
+    return FFG_OK;
 }
 
 int ffg_majorana_propagate(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im,
@@ -2811,6 +3029,13 @@ int64_t ffg_pauli_schedule(const ffg_pauli_gate* gates, size_t ngates, int batch
 int ffg_pauli_propagate_batched(ffg_ctx* ctx, const uint64_t* keys, const double* re, size_t n,
                                 const ffg_pauli_gate* gates, size_t ngates, const ffg_pauli_params* params,
                                 const ffg_batch_params* bp, double* expect, ffg_batch** out) {
+    return ffg_pauli_propagate_instances(ctx, keys, re, n, gates, ngates, params, bp, nullptr, expect, out);
+}
+
+int ffg_pauli_propagate_instances(ffg_ctx* ctx, const uint64_t* keys, const double* re, size_t n,
+                                  const ffg_pauli_gate* gates, size_t ngates, const ffg_pauli_params* params,
+                                  const ffg_batch_params* bp, const uint64_t* active, double* expect,
+                                  ffg_batch** out) {
     if (!ctx || !params || !bp || !expect || (n && (!keys || !re)) || (ngates && !gates)) return FFG_ERR_ARG;
     if (out) *out = nullptr;
     const size_t ninst = bp->ninst;
@@ -2824,6 +3049,8 @@ int ffg_pauli_propagate_batched(ffg_ctx* ctx, const uint64_t* keys, const double
     if (params->max_xweight >= 0)
         return set_err(ctx, FFG_ERR_ARG, "batched propagation does not support X-weight truncation");
     if (bp->checkpoint_every < 0) return set_err(ctx, FFG_ERR_ARG, "checkpoint_every must be >= 0");
+    if (active && bp->checkpoint_every > 0)
+        return set_err(ctx, FFG_ERR_ARG, "per-instance active rotations do not support the adjoint");
     if (ctx->group_d != 1 || !ctx->orbit || !ctx->persistent)
         return set_err(ctx, FFG_ERR_ARG, "batched propagation needs the orbit and persistent paths (FFG_* overrides)");
     for (size_t i = 0; i < n; i++)
@@ -2934,6 +3161,14 @@ int ffg_pauli_propagate_batched(ffg_ctx* ctx, const uint64_t* keys, const double
         if (!cs.empty())
             CK(cudaMemcpy(h->d_inst_cs, cs.data(), cs.size() * sizeof(double2), cudaMemcpyHostToDevice));
         h->bc.d_inst_cs = h->d_inst_cs;
+        h->bc.nrot = (u32)nrot;
+        if (active) {
+            const size_t words = std::max<size_t>((nrot + 63) / 64, 1);
+            CK(cudaMalloc(&h->d_active, ninst * words * 8));
+            CK(cudaMemcpy(h->d_active, active, ninst * words * 8, cudaMemcpyHostToDevice));
+            h->bc.d_active = h->d_active;
+            h->bc.active_words = (u32)words;
+        }
         int rc = upload_cliffords(ctx, gates, ngates);
         if (rc) return rc;
         rc = kw == 2 ? batch_forward<2>(h, ek.data(), re, n, expect) : batch_forward<4>(h, ek.data(), re, n, expect);
@@ -2991,6 +3226,7 @@ void ffg_batch_free(ffg_batch* h) {
     if (h->fkey) cudaFree(h->fkey);
     if (h->fre) cudaFree(h->fre);
     if (h->d_inst_cs) cudaFree(h->d_inst_cs);
+    if (h->d_active) cudaFree(h->d_active);
     delete h;
 }
 
@@ -3237,6 +3473,24 @@ const OptionRef kOptions[] = {
      [](ffg_ctx* c, int64_t v) { if (v < 1) return false; c->morbit_min_gates = (int)v; return true; }},
     {"morbit_route_big", [](const ffg_ctx* c) { return c->morbit_route_big; },
      [](ffg_ctx* c, int64_t v) { if (v < 1 || v > 1 << 20) return false; c->morbit_route_big = (int)v; return true; }},
+    {"min_capacity", [](const ffg_ctx* c) { return (int)c->min_capacity; },
+     [](ffg_ctx* c, int64_t v) {
+         if (v < 64 || v > (1ll << 30) || (v & (v - 1))) return false;
+         c->min_capacity = (u64)v;
+         return true;
+     }},
+    {"store_headroom", [](const ffg_ctx* c) { return c->store_headroom; },
+     [](ffg_ctx* c, int64_t v) {
+         if (v < 1 || v > 64) return false;
+         c->store_headroom = (int)v;
+         return true;
+     }},
+    {"group_region_cap", [](const ffg_ctx* c) { return (int)c->group_region_cap; },
+     [](ffg_ctx* c, int64_t v) {
+         if (v < 64 || v > (1ll << 24) || (v & (v - 1))) return false;
+         c->group_region_cap = (u64)v;
+         return true;
+     }},
 };
 }  // namespace
 

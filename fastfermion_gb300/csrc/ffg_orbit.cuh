@@ -46,7 +46,7 @@ struct BatchGate {
     u64 p[4];     // axis planes in store order (the NW x words, then the NW z words)
     double c, s;
     int yP;
-    int pad;
+    int gidx;     // index of the gate in the caller's circuit (capture records)
 };
 
 struct OrbitScratch {
@@ -105,6 +105,27 @@ struct OrbitCounters {
 #define OCHK(cond, code, a_, b_, c_)
 #endif
 
+// Partners that the degree filter drops, recorded for the learned correction
+// (no counterpart in the reference): every partner of degree in
+// (maxdeg of the batch, cap.maxdeg] whose |value| exceeds cap.min_abs (every
+// one when min_abs is 0), with the
+// index of the circuit gate that created it.  A group or batch that is run
+// again (a table or the output store overflowed) records its drops again; the
+// index over (key, gate) keeps the first record and marks later ones with
+// gate = -1.  Off when n is null.
+struct CaptureArgs {
+    u64* key;        // [4][cap] caller layout: xory words 0, 1, yorz words 0, 1
+    double* re;      // [cap]
+    double* im;      // [cap]
+    int* gate;       // [cap] circuit gate index, -1 = repeat of an earlier record
+    u32* slot;       // [2 * cap] index over (key, gate): record + 1, 0 = empty
+    u64* n;          // records claimed (> cap: the buffer was too small)
+    u64 cap;         // power of two
+    int maxdeg;
+    int pad;
+    double min_abs;
+};
+
 struct OrbitBatchArgs {
     const BatchGate* gates;  // k gates of the batch, application order
     int k;
@@ -126,7 +147,64 @@ struct OrbitBatchArgs {
     // qubit q are qidx[129 + qidx[q] .. 129 + qidx[q + 1]).  A Pauli gate
     // anticommutes only with terms whose support it touches.
     const u32* qidx;
+    // per-instance active rotations (null: every rotation acts on every
+    // instance).  Rotation r (circuit order among the rotations) acts on
+    // instance i iff bit r of active[i * active_words + r / 64]; batch gate t
+    // is rotation act_r0 - t.  An inactive gate leaves the instance's terms
+    // untouched; the batch-end truncation still runs.
+    const u64* active;
+    u32 active_words;
+    int act_r0;
+    CaptureArgs cap;
 };
+
+// whether batch gate t acts on instance inst
+__device__ __forceinline__ bool gate_active(const OrbitBatchArgs& a, u32 inst, int t) {
+    const int r = a.act_r0 - t;
+    return (__ldg(&a.active[(u64)inst * a.active_words + (u32)(r >> 6)]) >> (r & 63)) & 1ull;
+}
+
+template <int NW>
+__device__ __forceinline__ u64 capture_hash(const u64 (&c)[4], int gidx) {
+    u64 h = mix64(c[0] ^ 0x9e3779b97f4a7c15ull ^ ((u64)(u32)gidx << 32));
+#pragma unroll
+    for (int w = 1; w < 4; w++) h = mix64(h ^ c[w]);
+    return h;
+}
+
+// Records one dropped partner (key k in store order, value v) created by the
+// circuit gate gidx.
+template <int NW, bool CPLX>
+__device__ void capture_drop(const CaptureArgs& cp, const u64* k, cplx v, int gidx) {
+    if (cp.min_abs > 0.0) {  // min_abs = 0 records every dropped partner, exact zeros included
+        const bool small = CPLX ? abs_le(v.re, v.im, cp.min_abs) : (fabs(v.re) <= cp.min_abs);
+        if (small) return;
+    }
+    const u64 idx = atomicAdd(cp.n, 1ull);
+    if (idx >= cp.cap) return;  // the host sees n > cap and runs again with more room
+    const u64 c[4] = {k[0], NW == 2 ? k[1] : 0ull, k[NW], NW == 2 ? k[NW + 1] : 0ull};
+#pragma unroll
+    for (int w = 0; w < 4; w++) cp.key[(u64)w * cp.cap + idx] = c[w];
+    cp.re[idx] = v.re;
+    cp.im[idx] = CPLX ? v.im : 0.0;
+    cp.gate[idx] = gidx;
+    __threadfence();
+    const u64 mask = 2 * cp.cap - 1;
+    u64 pos = capture_hash<NW>(c, gidx) & mask;
+    for (u64 probe = 0; probe <= mask; probe++) {
+        const u32 e = atomicCAS(&cp.slot[pos], 0u, (u32)idx + 1u);
+        if (e == 0u) return;
+        const u64 j = e - 1u;
+        bool same = __ldcg(&cp.gate[j]) == gidx;
+#pragma unroll
+        for (int w = 0; w < 4; w++) same = same && __ldcg(&cp.key[(u64)w * cp.cap + j]) == c[w];
+        if (same) {
+            cp.gate[idx] = -1;
+            return;
+        }
+        pos = (pos + 1) & mask;
+    }
+}
 
 // Waits until the grid this one depends on (programmatic dependent launch)
 // has completed and its memory is visible; returns at once for a normal launch.
@@ -249,6 +327,7 @@ __global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, StoreView
         load_key<KW>(in, i, q);
         u64 A[kAW] = {};
         u64 U[KW] = {};
+        const u32 inst = a.active ? (u32)((q[a.inst_plane] >> a.inst_shift) & a.inst_mask) : 0u;
         if (a.qidx) {
             // candidates: the gates on the term's support
 #pragma unroll
@@ -261,6 +340,7 @@ __global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, StoreView
                     for (u32 e = __ldg(&a.qidx[qb]); e < e1; e++) {
                         const int t = (int)__ldg(&a.qidx[129 + e]);
                         if ((A[t >> 6] >> (t & 63)) & 1ull) continue;
+                        if (a.active && !gate_active(a, inst, t)) continue;
                         u64 par = 0;
 #pragma unroll
                         for (int w = 0; w < NW; w++) par ^= (q[w] & gp[t][NW + w]) ^ (q[NW + w] & gp[t][w]);
@@ -274,6 +354,7 @@ __global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, StoreView
             }
         } else {
             for (int t = 0; t < a.k; t++) {
+                if (a.active && !gate_active(a, inst, t)) continue;
                 u64 par = 0;
 #pragma unroll
                 for (int w = 0; w < NW; w++) par ^= (q[w] & gp[t][NW + w]) ^ (q[NW + w] & gp[t][w]);
@@ -559,7 +640,11 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                         const cplx cj = {T.re[j], CPLX ? T.im[j] : 0.0};
                         cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
                         if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
+                        else if (a.cap.n && dQ <= a.cap.maxdeg)
+                            capture_drop<NW, CPLX>(a.cap, q, rot_partner<CPLX>(cj, gs, jK), G.gidx);
                         if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
+                        else if (a.cap.n && dK <= a.cap.maxdeg)
+                            capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), G.gidx);
                         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
                         T.re[m] = ni.re;
                         T.re[j] = nj.re;
@@ -587,6 +672,8 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                                 g_created++;
                                 g_xapps += a.k - 1 - t;
                             }
+                        } else if (a.cap.n && dK <= a.cap.maxdeg) {
+                            capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), G.gidx);
                         }
                     }
                 }
@@ -826,7 +913,11 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                         const cplx cj = {tld<SM>(&G.re[j]), CPLX ? tld<SM>(&G.im[j]) : 0.0};
                         cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
                         if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
+                        else if (a.cap.n && dQ <= a.cap.maxdeg)
+                            capture_drop<NW, CPLX>(a.cap, q, rot_partner<CPLX>(cj, gs, jK), Gt.gidx);
                         if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
+                        else if (a.cap.n && dK <= a.cap.maxdeg)
+                            capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
                         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
                         G.re[m] = ni.re;
                         G.re[j] = nj.re;
@@ -854,6 +945,8 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                                 g_created++;
                                 g_xapps += a.k - 1 - t;
                             }
+                        } else if (a.cap.n && dK <= a.cap.maxdeg) {
+                            capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
                         }
                     }
                 }

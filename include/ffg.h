@@ -146,6 +146,14 @@ void* ffg_stream(const ffg_ctx* ctx);
  *   morbit_route_big  |A| from which a Majorana group skips the warp tier (12)
  *   merge_sort        1: Pauli rotations one at a time with a radix sort and a
  *                     segmented reduce instead of the hash index / orbit paths (0)
+ *   min_capacity      smallest term-store capacity, a power of two >= 64 (65536)
+ *   store_headroom    orbit windows size their output stores for this many times
+ *                     the entering terms, 1..64 (4); a batch that outgrows its
+ *                     store runs again after the store grows
+ *   group_region_cap  members of the first global-memory region of a group too
+ *                     large for shared memory, a power of two >= 64 (16384; the
+ *                     Majorana path starts at a quarter); regions grow x4 on
+ *                     overflow and the group runs again
  * Results do not depend on the options (only speed does). */
 int ffg_set_option(ffg_ctx* ctx, const char* name, int64_t value);
 int ffg_get_option(const ffg_ctx* ctx, const char* name, int64_t* value);
@@ -238,6 +246,22 @@ typedef struct {
 int ffg_pauli_propagate_batched(ffg_ctx* ctx, const uint64_t* keys, const double* re, size_t n,
                                 const ffg_pauli_gate* gates, size_t ngates, const ffg_pauli_params* params,
                                 const ffg_batch_params* bparams, double* expect, ffg_batch** out);
+/* ffg_pauli_propagate_instances: ffg_pauli_propagate_batched with, in
+ * addition, a per-instance choice of the rotations that act.  active is NULL
+ * (every rotation acts on every instance) or an array [ninst][W], W =
+ * max(1, ceil(nrot / 64)) words: rotation r (the r-th FFG_ROT gate in circuit
+ * order) acts on instance i iff bit r % 64 of active[i * W + r / 64] is set.
+ * An inactive rotation leaves the instance's terms as they are; Clifford gates
+ * act on every instance, and the truncation points are those of the whole
+ * circuit (after each commuting run of its rotations), so each instance's term
+ * set is that of the whole circuit with its inactive rotations skipped.  Not
+ * combinable with the adjoint (checkpoint_every must be 0 when active is set).
+ * The learned correction uses it to propagate every dropped partner from the
+ * gate that created it, all partners in one launch. */
+int ffg_pauli_propagate_instances(ffg_ctx* ctx, const uint64_t* keys, const double* re, size_t n,
+                                  const ffg_pauli_gate* gates, size_t ngates, const ffg_pauli_params* params,
+                                  const ffg_batch_params* bparams, const uint64_t* active, double* expect,
+                                  ffg_batch** out);
 /* Terms left over all instances. */
 size_t ffg_batch_size(const ffg_batch* b);
 /* Final terms: keys [4][n] (caller layout, instance code removed), re[n],
@@ -250,6 +274,84 @@ int ffg_batch_copy(const ffg_batch* b, uint64_t* keys, double* re, int64_t* inst
  * with; may run any number of times. */
 int ffg_batch_adjoint(ffg_batch* b, const double* weights, double* grad_theta, double* grad_coef);
 void ffg_batch_free(ffg_batch* b);
+
+/* -------------------------------------------------------------------------- */
+/* Dropped partners (training data of the learned correction).  No counterpart
+ * in the reference, whose conjugate (src/pauli/propagate.h:71-89) discards
+ * them.  ffg_pauli_propagate_capture runs ffg_pauli_propagate (batched mode
+ * without top-k; the result is identical) and also records every partner that
+ * the degree filter drops whose degree is at most capdeg (> maxdegree) and
+ * whose |value| exceeds min_abs (min_abs = 0: every one, exact zeros
+ * included): its key, its value c (i sin theta) phase(P Q),
+ * and the index in gates[] of the rotation that created it (the gates still
+ * to be applied to it are gates[0 .. gate)).  Each (key, gate) is recorded
+ * once.  *drops stays valid until ffg_drops_free; ffg_drops_copy returns the
+ * records sorted by gate, then key (keys [4][n] caller layout). */
+typedef struct ffg_drops ffg_drops;
+int ffg_pauli_propagate_capture(ffg_ctx* ctx, const uint64_t* keys, const double* re, const double* im,
+                                size_t n, const ffg_pauli_gate* gates, size_t ngates,
+                                const ffg_pauli_params* params, int on_device, int32_t capdeg, double min_abs,
+                                ffg_result** out, ffg_drops** drops);
+size_t ffg_drops_size(const ffg_drops* d);
+int ffg_drops_copy(const ffg_drops* d, uint64_t* keys, double* re, double* im, int32_t* gate);
+/* Device arrays of the records, in no particular order: key plane w at
+ * keys + w * stride (stride = size), re, im, gate. */
+int ffg_drops_device(const ffg_drops* d, const uint64_t** keys, size_t* stride, const double** re,
+                     const double** im, const int32_t** gate);
+void ffg_drops_free(ffg_drops* d);
+
+/* -------------------------------------------------------------------------- */
+/* Learned truncation correction: the surrogate network and the features of
+ * dropped partners.  No counterpart in the reference.
+ *
+ * The network maps the 32 features of a dropped partner to its transfer t,
+ * the value at the end of the circuit of the partner with unit coefficient:
+ * 32 -> 128 -> 128 -> 128 -> 1, GELU after each hidden layer.  The three
+ * hidden GEMMs run on the tensor cores (tcgen05, BF16 operands, FP32
+ * accumulation in tensor memory); the output layer, biases, activations and
+ * the optimizer are FP32.  Parameters (FP32, FFG_MLP_NPARAMS values) are laid
+ * out as W1[128][32], b1[128], W2[128][128], b2[128], W3[128][128], b3[128],
+ * w4[128], b4 (weights as [out][in]).  A network uses its context's stream;
+ * create it with the context's device current.  x arrays are device BF16
+ * (uint16 bit patterns) [n][32], row-major, 16-byte aligned; target, weight
+ * and y are device FP32 [n].  The training loss is
+ * L = sum_r weight[r] (y[r] - target[r])^2. */
+#define FFG_MLP_IN 32
+#define FFG_MLP_HIDDEN 128
+#define FFG_MLP_NPARAMS 37377
+typedef struct ffg_mlp ffg_mlp;
+int ffg_mlp_create(ffg_ctx* ctx, ffg_mlp** out);
+void ffg_mlp_free(ffg_mlp* m);
+const char* ffg_mlp_last_error(const ffg_mlp* m);
+/* Host FP32 parameters in and out (set_params also resets the optimizer). */
+int ffg_mlp_set_params(ffg_mlp* m, const float* params);
+int ffg_mlp_get_params(const ffg_mlp* m, float* params);
+/* y = f(x) for n rows. */
+int ffg_mlp_forward(ffg_mlp* m, const uint16_t* x, size_t n, float* y);
+/* dL/dparams over n rows into the host array grad, and L (may be NULL). */
+int ffg_mlp_gradient(ffg_mlp* m, const uint16_t* x, const float* target, const float* weight, size_t n,
+                     float* grad, double* loss);
+/* One Adam step on L over n rows; *loss (may be NULL: no synchronisation)
+ * receives L before the step. */
+int ffg_mlp_adam_step(ffg_mlp* m, const uint16_t* x, const float* target, const float* weight, size_t n,
+                      float lr, float beta1, float beta2, float eps, double* loss);
+/* Predicted correction sum_r coef[r] t[r] (coef device FP64 [n]); t receives
+ * the n transfers. */
+int ffg_mlp_correction(ffg_mlp* m, const uint16_t* x, const double* coef, size_t n, float* t, double* out);
+/* Self-test of the tensor-core path: D[128][N] = A[128][K] B[N][K]^T with host
+ * BF16 A, B and FP32 D (K in 16..128, N in 16..256, multiples of 16). */
+int ffg_mlp_selftest_gemm(ffg_mlp* m, int N, int K, const uint16_t* a, const uint16_t* b, float* d);
+/* Features of n dropped partners (device keys [4][stride], coef = real parts,
+ * gate = creating gate) of the circuit gates[0..ngates) (host): batch_of_gate
+ * (host, [ngates]) is the commuting run of each gate in application order
+ * (nbatches runs), coords (host, [2][128]) the lattice coordinates of the
+ * qubits, obs_qubit the observable's site, maxdegree the cutoff that dropped
+ * them.  Writes FP32 features feat[n][32] and/or BF16 x[n][32] (device, either
+ * may be NULL). */
+int ffg_drop_features(ffg_ctx* ctx, const uint64_t* keys, size_t stride, const double* coef, const int32_t* gate,
+                      size_t n, const ffg_pauli_gate* gates, size_t ngates, const int32_t* batch_of_gate,
+                      int32_t nbatches, const float* coords, int32_t obs_qubit, int32_t maxdegree, float* feat,
+                      uint16_t* x);
 
 /* -------------------------------------------------------------------------- */
 /* Allocation-free rotations.  No counterpart in the reference: this entry

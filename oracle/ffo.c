@@ -495,11 +495,17 @@ typedef struct {
     int rot_count;
     int64_t apps, peak;
     ffo_drops* drops; /* serial strategy only */
+    const uint64_t* active;  /* per-rotation mask (NULL: every rotation acts) */
+    const int64_t* rot_of;   /* circuit gate index -> rotation index */
 } pdrv_t;
 
 static int64_t drv_size(pdrv_t* D) { return D->S ? shards_size(D->S) : D->m->d.n; }
 
 static void drv_rot(pdrv_t* D, int64_t gi) {
+    if (D->active) { /* an inactive rotation leaves the terms as they are */
+        const int64_t r = D->rot_of[gi];
+        if (!((D->active[r >> 6] >> (r & 63)) & 1ULL)) return;
+    }
     D->apps += drv_size(D);
     if (D->S)
         pauli_conjugate_sharded(D->S, &D->gates[gi], D->p->maxdegree);
@@ -557,7 +563,7 @@ static int valid_qubit(int q) { return q >= 0 && q < 128; }
 
 static ffo_poly* pauli_propagate(const ffo_pauli_gate* gates, int64_t ngates, const uint64_t* keys,
                                  const double* re, const double* im, int64_t n, const ffo_pauli_params* p,
-                                 ffo_drops* drops) {
+                                 ffo_drops* drops, const uint64_t* active) {
     for (int64_t i = 0; i < ngates; i++) {
         const ffo_pauli_gate* g = &gates[i];
         if (g->kind < 0 || g->kind > FFO_CZ) return NULL;
@@ -578,6 +584,14 @@ static ffo_poly* pauli_propagate(const ffo_pauli_gate* gates, int64_t ngates, co
     D.gates = gates;
     D.p = p;
     D.drops = drops;
+    D.active = active;
+    int64_t* rot_of = NULL;
+    if (active) {
+        rot_of = (int64_t*)malloc((size_t)(ngates > 0 ? ngates : 1) * sizeof(int64_t));
+        int64_t r = 0;
+        for (int64_t i = 0; i < ngates; i++) rot_of[i] = gates[i].kind == FFO_ROT ? r++ : -1;
+        D.rot_of = rot_of;
+    }
     D.m = &out->m;
     D.peak = out->m.d.n;
     if (T > 1) {
@@ -638,6 +652,7 @@ static ffo_poly* pauli_propagate(const ffo_pauli_gate* gates, int64_t ngates, co
         free(S.sh);
     }
     free(D.nb.v);
+    free(rot_of);
     out->apps = D.apps;
     out->peak = D.peak;
     return out;
@@ -646,7 +661,13 @@ static ffo_poly* pauli_propagate(const ffo_pauli_gate* gates, int64_t ngates, co
 ffo_poly* ffo_pauli_propagate(const ffo_pauli_gate* gates, int64_t ngates, const uint64_t* keys,
                               const double* re, const double* im, int64_t n,
                               const ffo_pauli_params* p) {
-    return pauli_propagate(gates, ngates, keys, re, im, n, p, NULL);
+    return pauli_propagate(gates, ngates, keys, re, im, n, p, NULL, NULL);
+}
+
+ffo_poly* ffo_pauli_propagate_masked(const ffo_pauli_gate* gates, int64_t ngates, const uint64_t* keys,
+                                     const double* re, const double* im, int64_t n,
+                                     const ffo_pauli_params* p, const uint64_t* active) {
+    return pauli_propagate(gates, ngates, keys, re, im, n, p, NULL, active);
 }
 
 ffo_poly* ffo_pauli_propagate_capture(const ffo_pauli_gate* gates, int64_t ngates, const uint64_t* keys,
@@ -654,7 +675,7 @@ ffo_poly* ffo_pauli_propagate_capture(const ffo_pauli_gate* gates, int64_t ngate
                                       const ffo_pauli_params* p, int32_t capdeg, ffo_drops** dropped) {
     ffo_drops* d = (ffo_drops*)calloc(1, sizeof(ffo_drops));
     d->capdeg = capdeg;
-    ffo_poly* r = pauli_propagate(gates, ngates, keys, re, im, n, p, d);
+    ffo_poly* r = pauli_propagate(gates, ngates, keys, re, im, n, p, d, NULL);
     if (!r) {
         ffo_drops_free(d);
         d = NULL;

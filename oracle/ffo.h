@@ -68,6 +68,15 @@ ffo_poly* ffo_pauli_propagate_capture(const ffo_pauli_gate* gates, int64_t ngate
                                       const uint64_t* keys, const double* re, const double* im,
                                       int64_t n, const ffo_pauli_params* p, int32_t capdeg,
                                       ffo_drops** dropped);
+/* Propagation with some rotations skipped (not a reference feature: the
+ * semantics of one instance of the GPU's per-instance active rotations).
+ * Rotation r (circuit order among the ROT gates) acts iff bit r % 64 of
+ * active[r / 64] is set; an inactive rotation leaves the terms as they are,
+ * while batching and truncation points stay those of the whole circuit.
+ * Serial and sharded strategies as in ffo_pauli_propagate. */
+ffo_poly* ffo_pauli_propagate_masked(const ffo_pauli_gate* gates, int64_t ngates,
+                                     const uint64_t* keys, const double* re, const double* im,
+                                     int64_t n, const ffo_pauli_params* p, const uint64_t* active);
 int64_t ffo_drops_size(const ffo_drops* d);
 void ffo_drops_copy(const ffo_drops* d, uint64_t* keys /* [4][n] */, double* re, double* im,
                     int64_t* gate);

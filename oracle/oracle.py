@@ -66,6 +66,8 @@ def lib():
         L.ffo_pauli_propagate_capture.restype = vp
         L.ffo_pauli_propagate_capture.argtypes = [vp, i64, vp, vp, vp, i64, ctypes.POINTER(_Params),
                                                   ctypes.c_int32, ctypes.POINTER(vp)]
+        L.ffo_pauli_propagate_masked.restype = vp
+        L.ffo_pauli_propagate_masked.argtypes = [vp, i64, vp, vp, vp, i64, ctypes.POINTER(_Params), vp]
         L.ffo_drops_size.restype = i64
         L.ffo_drops_size.argtypes = [vp]
         L.ffo_drops_copy.argtypes = [vp, vp, vp, vp, vp]
@@ -119,15 +121,25 @@ class OraclePoly:
 
 
 def pauli_propagate(gates, keys, re, im=None, maxdegree=128, mincoeff=0.0, topk=0,
-                    max_xweight=-1, xtrunc_period=1, batched=True, n_threads=1):
+                    max_xweight=-1, xtrunc_period=1, batched=True, n_threads=1, active=None):
+    """active: None, or a uint64 mask over the rotations (bit r of word r // 64
+    set = the r-th ROT gate in circuit order acts; the others are skipped, the
+    batching and truncation points stay those of the whole circuit)."""
     gates = np.ascontiguousarray(gates, dtype=PAULI_GATE)
     keys = np.ascontiguousarray(keys, dtype=np.uint64).reshape(4, -1)
     re = np.ascontiguousarray(re, dtype=np.float64)
     im = None if im is None else np.ascontiguousarray(im, dtype=np.float64)
     p = _Params(int(maxdegree), int(topk), float(mincoeff), int(max_xweight),
                 int(xtrunc_period), int(bool(batched)), int(n_threads))
-    h = lib().ffo_pauli_propagate(_ptr(gates), gates.size, _ptr(keys), _ptr(re), _ptr(im),
-                                  re.size, ctypes.byref(p))
+    if active is not None:
+        nrot = int(np.count_nonzero(gates["kind"] == ROT))
+        active = np.ascontiguousarray(active, dtype=np.uint64).reshape(-1)
+        assert active.size >= max(1, (nrot + 63) // 64)
+        h = lib().ffo_pauli_propagate_masked(_ptr(gates), gates.size, _ptr(keys), _ptr(re), _ptr(im),
+                                             re.size, ctypes.byref(p), _ptr(active))
+    else:
+        h = lib().ffo_pauli_propagate(_ptr(gates), gates.size, _ptr(keys), _ptr(re), _ptr(im),
+                                      re.size, ctypes.byref(p))
     if not h:
         raise ValueError("oracle rejected the circuit")
     return OraclePoly(h)
