@@ -51,6 +51,38 @@ def build(force=False, verbose=False):
     return LIB
 
 
+STAGE = os.path.join(os.path.dirname(HERE), "baseline", "_ref")
+BINDING_SRC = os.path.join(HERE, "binding", "ffcore_gpu.cpp")
+
+
+def binding_path():
+    import sysconfig
+    return os.path.join(HERE, "binding", "ffcore_gpu" + sysconfig.get_config_var("EXT_SUFFIX"))
+
+
+def build_binding(force=False):
+    """Compiles the drop-in module ffcore_gpu (fastfermion's propagate on libffg)
+    against the reference headers and pybind11 staged in baseline/_ref; returns
+    its path, or None when they are not staged on this machine."""
+    import sysconfig
+    src_inc = os.path.join(STAGE, "_src", "src")
+    pyb_inc = os.path.join(STAGE, "_pybind11", "include")
+    if not (os.path.isdir(src_inc) and os.path.isdir(pyb_inc)):
+        return None
+    out = binding_path()
+    lib = build()
+    deps = [BINDING_SRC, lib, os.path.join(os.path.dirname(HERE), "include", "ffg.h")]
+    if not force and os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+        return out
+    cmd = ["g++", "-O3", "-std=c++20", "-shared", "-fPIC", "-fopenmp", "-DFF_OPENMP", '-DFF_VERSION="ref"',
+           "-ffp-contract=off", "-w", f"-I{src_inc}", f"-I{os.path.join(src_inc, 'hashmap')}", f"-I{pyb_inc}",
+           f"-I{sysconfig.get_paths()['include']}", f"-I{os.path.join(os.path.dirname(HERE), 'include')}",
+           BINDING_SRC, f"-L{HERE}", "-lffg", "-Wl,-rpath,$ORIGIN/..", "-o", out + ".tmp"]
+    subprocess.run(cmd, check=True)
+    os.replace(out + ".tmp", out)
+    return out
+
+
 if __name__ == "__main__":
     import sys
     build(force=True, verbose="-v" in sys.argv)

@@ -56,6 +56,19 @@ def kicked_ising_circuit(theta_h, lx=10, ly=10, steps=20, theta_zz=-math.pi / 2)
 KICKED_ISING_THETAS = (0.1, 0.3, 0.5, 0.7, 0.9, 1.1, math.pi / 2)
 
 
+def learned_correction_thetas(seed=2024):
+    """theta_h values of the learned-correction workload on the 10x10 kicked
+    Ising circuit: a seeded training grid of 64 values in [0.05, pi/2] (64
+    equal cells, one uniform draw in each) and 16 held-out values drawn
+    uniformly from the same range."""
+    rng = np.random.default_rng(seed)
+    lo, hi = 0.05, math.pi / 2
+    edges = np.linspace(lo, hi, 65)
+    train = edges[:-1] + rng.uniform(0.0, 1.0, 64) * np.diff(edges)
+    held = np.sort(rng.uniform(lo, hi, 16))
+    return [float(t) for t in train], [float(t) for t in held]
+
+
 def hubbard_step(lx=6, ly=6, t=1.0, u=4.0, dt=0.1):
     """One Trotter step of the spinful 2D Fermi-Hubbard model in Majorana form.
 
