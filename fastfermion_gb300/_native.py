@@ -61,7 +61,8 @@ EXPORTS = ["ffg_create", "ffg_destroy", "ffg_last_error", "ffg_set_profiling", "
            "ffg_get_option", "ffg_pauli_propagate_instances", "ffg_pauli_propagate_capture", "ffg_drops_size",
            "ffg_drops_copy", "ffg_drops_device", "ffg_drops_free", "ffg_mlp_create", "ffg_mlp_free",
            "ffg_mlp_last_error", "ffg_mlp_set_params", "ffg_mlp_get_params", "ffg_mlp_forward", "ffg_mlp_gradient",
-           "ffg_mlp_adam_step", "ffg_mlp_correction", "ffg_mlp_selftest_gemm", "ffg_drop_features"]
+           "ffg_mlp_adam_step", "ffg_mlp_correction", "ffg_mlp_selftest_gemm", "ffg_drop_features",
+           "ffg_mlp_set_targets"]
 
 MLP_IN, MLP_HIDDEN, MLP_NPARAMS = 32, 128, 37377
 
@@ -127,9 +128,10 @@ def lib():
             L.ffg_mlp_adam_step.argtypes = [vp, vp, vp, vp, sz, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                             ctypes.c_float, dp]
             L.ffg_mlp_correction.argtypes = [vp, vp, vp, sz, vp, dp]
+            L.ffg_mlp_set_targets.argtypes = [vp, vp, sz, vp, vp, vp, sz, vp, vp, vp, vp, vp]
             L.ffg_mlp_selftest_gemm.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp]
             L.ffg_drop_features.argtypes = [vp, vp, sz, vp, vp, sz, vp, sz, vp, ctypes.c_int32, vp, ctypes.c_int32,
-                                            ctypes.c_int32, vp, vp]
+                                            ctypes.c_int32, vp, vp, vp, vp]
             L.ffg_batch_size.restype = sz
             L.ffg_batch_size.argtypes = [vp]
             L.ffg_batch_copy.argtypes = [vp, vp, vp, vp]
@@ -175,7 +177,8 @@ class Context:
 
     OPTIONS = ("orbit_route_big", "orbit_team", "orbit_window", "orbit_min_gates", "orbit_qidx", "pdl",
                "morbit", "morbit_min_gates", "morbit_route_big", "merge_sort", "orbit_team_threads",
-               "orbit_block_threads", "min_capacity", "store_headroom", "group_region_cap")
+               "orbit_block_threads", "min_capacity", "store_headroom", "group_region_cap",
+               "barrier_limit_kcycles")
 
     def set_option(self, name, value):
         self.check(self.L.ffg_set_option(self.h, name.encode(), int(value)))
@@ -358,6 +361,26 @@ def _dptr(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
+class _CudaArray:
+    """A device array by address (CUDA array interface), for zero-copy torch views."""
+
+    def __init__(self, addr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(addr), False),
+                                         "version": 2}
+
+
+def device_view(addr, shape, typestr):
+    """torch view of device memory owned by libffg (keep the owner alive)."""
+    import torch
+    return torch.as_tensor(_CudaArray(addr, shape, typestr), device="cuda")
+
+
+def device_copy(dst, src, nbytes):
+    """Device-to-device copy of nbytes between two addresses."""
+    if nbytes:
+        device_view(dst, (nbytes,), "|u1").copy_(device_view(src, (nbytes,), "|u1"))
+
+
 class MLP:
     """The surrogate network of the learned correction (ffg_mlp), on a context's
     stream.  Device arrays are torch CUDA tensors (or integer addresses): x BF16
@@ -409,6 +432,15 @@ class MLP:
         self.check(self.L.ffg_mlp_correction(self.h, _dptr(x), _dptr(coef), int(n), _dptr(t), ctypes.byref(out)))
         return out.value
 
+    def set_targets(self, x, n, coef, seg, delta, nseg, target, weight, label=None, label_weight=None,
+                    want_loss=False):
+        """ffg_mlp_set_targets; returns (set loss, label loss) when want_loss."""
+        loss = (ctypes.c_double * 2)()
+        self.check(self.L.ffg_mlp_set_targets(self.h, _dptr(x), int(n), _dptr(coef), _dptr(seg), _dptr(delta),
+                                              int(nseg), _dptr(label), _dptr(label_weight), _dptr(target),
+                                              _dptr(weight), loss if want_loss else None))
+        return (loss[0], loss[1]) if want_loss else None
+
     def selftest_gemm(self, a_bits, b_bits):
         """D = A B^T for host BF16 bit patterns A (128, K), B (N, K) -> (128, N)"""
         a = np.ascontiguousarray(a_bits, dtype=np.uint16)
@@ -431,14 +463,17 @@ class MLP:
 
 
 def drop_features(ctx, keys, stride, coef, gate, n, gates, batch_of_gate, nbatches, coords, obs, maxdegree,
-                  feat=None, x=None):
-    """ffg_drop_features on device arrays (torch tensors or addresses)."""
+                  feat=None, x=None, shift=None, scale=None):
+    """ffg_drop_features on device arrays (torch tensors or addresses); shift and
+    scale (host, 32 values) standardise the BF16 input x."""
     gates = np.ascontiguousarray(gates, dtype=PAULI_GATE)
     bog = np.ascontiguousarray(batch_of_gate, dtype=np.int32)
     co = np.ascontiguousarray(coords, dtype=np.float32).reshape(2, 128)
+    sh = None if shift is None else np.ascontiguousarray(shift, dtype=np.float32)
+    sc = None if scale is None else np.ascontiguousarray(scale, dtype=np.float32)
     ctx.check(ctx.L.ffg_drop_features(ctx.h, _dptr(keys), int(stride), _dptr(coef), _dptr(gate), int(n),
                                       _ptr(gates), gates.size, _ptr(bog), int(nbatches), _ptr(co), int(obs),
-                                      int(maxdegree), _dptr(feat), _dptr(x)))
+                                      int(maxdegree), _ptr(sh), _ptr(sc), _dptr(feat), _dptr(x)))
 
 
 class Drops:

@@ -192,6 +192,7 @@ struct ffg_ctx {
     size_t smscratch_bytes = 0;
     int morbit_min_gates = 2;   // shortest Majorana run sent to the batch-orbit path
     u64 min_capacity = 1ull << 16;      // smallest term-store capacity (option min_capacity)
+    long long barrier_limit = kBarrierLimitCycles;  // grid-barrier wait limit, cycles (option barrier_limit_kcycles)
     int store_headroom = 4;             // orbit windows size their stores for this many times
                                         // the entering terms (option store_headroom)
     u64 group_region_cap = 1ull << 14;  // members of a first global-memory group region (Pauli;
@@ -808,6 +809,7 @@ struct Engine {
             pa.op_begin = (int)i;
             pa.op_end = (int)end;
             pa.compact_min = 4096;
+            pa.barrier_limit = ctx->barrier_limit;
             StoreView v = cur.v;
             DevCounters* C = ctx->d_ctr;
             PersistState* ps = ctx->d_ps;
@@ -3477,6 +3479,12 @@ const OptionRef kOptions[] = {
      [](ffg_ctx* c, int64_t v) {
          if (v < 64 || v > (1ll << 30) || (v & (v - 1))) return false;
          c->min_capacity = (u64)v;
+         return true;
+     }},
+    {"barrier_limit_kcycles", [](const ffg_ctx* c) { return (int)(c->barrier_limit / 1000); },
+     [](ffg_ctx* c, int64_t v) {
+         if (v < 1 || v > kBarrierLimitCycles / 1000) return false;
+         c->barrier_limit = v * 1000;
          return true;
      }},
     {"store_headroom", [](const ffg_ctx* c) { return c->store_headroom; },

@@ -696,7 +696,9 @@ struct FeatArgs {
     const float* coords;   // [2][128] lattice coordinates of the qubits
     float lx, ly;          // lattice extents
     float* feat;           // [n][32] FP32 (may be null)
-    __nv_bfloat16* x;      // [n][32] BF16 (may be null)
+    __nv_bfloat16* x;      // [n][32] BF16 network input (may be null): (f - shift) * scale
+    const float* shift;    // [32] (null: 0)
+    const float* scale;    // [32] (null: 1)
 };
 
 __global__ void drop_features_kernel(FeatArgs A) {
@@ -796,9 +798,12 @@ __global__ void drop_features_kernel(FeatArgs A) {
     f[31] = (cy - oy) / A.ly;
     if (A.feat)
         for (int k = 0; k < 32; k++) A.feat[i * 32 + k] = f[k];
-    if (A.x)
+    if (A.x) {
+        if (A.shift)
+            for (int k = 0; k < 32; k++) f[k] = (f[k] - A.shift[k]) * A.scale[k];
         for (int k = 0; k < 32; k += 2)
             *reinterpret_cast<uint32_t*>(A.x + i * 32 + k) = pack_bf16(f[k], f[k + 1]);
+    }
 }
 
 // sum over rows of coef[r] * t[r] (the predicted correction), one block
@@ -813,6 +818,55 @@ __global__ void correction_sum_kernel(const double* coef, const float* t, size_t
         __syncthreads();
     }
     if (threadIdx.x == 0) *out = part[0];
+}
+
+// Set-level training targets.  For segments s (rows seg[s] .. seg[s+1]) with
+// targets delta[s] the loss is
+//     L = sum_s R_s^2 + sum_r lw_r (y_r - label_r)^2,  R_s = sum_{r in s} c_r y_r - delta_s,
+// so dL/dy_r = 2 R_s c_r + 2 lw_r (y_r - label_r).  The per-row training
+// kernel minimises sum_r w_r (y_r - t_r)^2, whose gradient is 2 w_r (y_r - t_r):
+// with w_r = omega + lw_r and t_r = y_r - (R_s c_r + lw_r (y_r - label_r)) / w_r
+// its step is a step on L.
+__global__ void segment_residual_kernel(const float* y, const double* coef, const int64_t* seg,
+                                        const double* delta, double* R, double* loss) {
+    __shared__ double part[256];
+    const int s = blockIdx.x;
+    double acc = 0.0;
+    for (int64_t r = seg[s] + threadIdx.x; r < seg[s + 1]; r += blockDim.x) acc += coef[r] * (double)y[r];
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double r = part[0] - delta[s];
+        R[s] = r;
+        atomicAdd(&loss[0], r * r);
+    }
+}
+
+__global__ void set_targets_kernel(const float* y, const double* coef, const int64_t* seg, int nseg,
+                                   const double* R, const float* label, const float* lw, float omega, size_t n,
+                                   float* target, float* weight, double* loss) {
+    const size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    int lo = 0, hi = nseg - 1;  // segment of row r: seg[lo] <= r < seg[lo + 1]
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (seg[mid] <= (int64_t)r) lo = mid;
+        else hi = mid - 1;
+    }
+    double g = R[lo] * coef[r];
+    float w = omega;
+    if (label) {
+        const float e = y[r] - label[r];
+        g += (double)lw[r] * e;
+        w += lw[r];
+        atomicAdd(&loss[1], (double)lw[r] * e * e);
+    }
+    weight[r] = w;
+    target[r] = (float)((double)y[r] - g / w);
 }
 
 // ---------------------------------------------------------------------------
@@ -841,6 +895,12 @@ struct ffg_mlp {
     // training scratch: h1, h2, dz1, dz2, dz3 ([rows][128] bf16 each)
     __nv_bfloat16* act = nullptr;
     size_t act_rows = 0;
+    // set-level targets: predictions, segment residuals, two loss terms
+    float* ys = nullptr;
+    size_t ys_rows = 0;
+    double* R = nullptr;
+    size_t R_segs = 0;
+    double* loss2 = nullptr;
     std::string err;
 };
 
@@ -964,7 +1024,7 @@ void ffg_mlp_free(ffg_mlp* m) {
     cudaSetDevice(m->device);
     if (m->stream) cudaStreamSynchronize(m->stream);
     for (void* p : {(void*)m->params, (void*)m->m, (void*)m->v, (void*)m->grad, (void*)m->img, (void*)m->loss,
-                    (void*)m->status, (void*)m->act})
+                    (void*)m->status, (void*)m->act, (void*)m->ys, (void*)m->R, (void*)m->loss2})
         if (p) cudaFree(p);
     delete m;
 }
@@ -1066,6 +1126,43 @@ int ffg_mlp_correction(ffg_mlp* m, const uint16_t* x, const double* coef, size_t
     return FFG_OK;
 }
 
+int ffg_mlp_set_targets(ffg_mlp* m, const uint16_t* x, size_t n, const double* coef, const int64_t* seg,
+                        const double* delta, size_t nseg, const float* label, const float* label_weight,
+                        float* target, float* weight, double* loss) {
+    if (!m || !n || !nseg || !x || !coef || !seg || !delta || !target || !weight || (label && !label_weight))
+        return FFG_ERR_ARG;
+    if (((uintptr_t)x & 15) != 0) return mlp_err(m, FFG_ERR_ARG, "x must be 16-byte aligned");
+    if (m->ys_rows < n) {
+        if (m->ys) MCK(cudaFree(m->ys));
+        m->ys = nullptr;
+        MCK(cudaMalloc(&m->ys, n * 4));
+        m->ys_rows = n;
+    }
+    if (m->R_segs < nseg) {
+        if (m->R) MCK(cudaFree(m->R));
+        m->R = nullptr;
+        MCK(cudaMalloc(&m->R, nseg * 8));
+        m->R_segs = nseg;
+    }
+    if (!m->loss2) MCK(cudaMalloc(&m->loss2, 16));
+    MCK(cudaMemsetAsync(m->loss2, 0, 16, m->stream));
+    mlp_forward_kernel<<<grid_rows(m, n), kThreads, sizeof(FwdSmem), m->stream>>>(
+        m->img, reinterpret_cast<const __nv_bfloat16*>(x), n, m->ys, m->status);
+    MCK(cudaGetLastError());
+    segment_residual_kernel<<<(unsigned)nseg, 256, 0, m->stream>>>(m->ys, coef, seg, delta, m->R, m->loss2);
+    MCK(cudaGetLastError());
+    set_targets_kernel<<<(unsigned)((n + 255) / 256), 256, 0, m->stream>>>(
+        m->ys, coef, seg, (int)nseg, m->R, label, label_weight, 1.0f / (float)n, n, target, weight, m->loss2);
+    MCK(cudaGetLastError());
+    if (loss) {
+        int rc = mlp_check_status(m);
+        if (rc) return rc;
+        MCK(cudaMemcpyAsync(loss, m->loss2, 16, cudaMemcpyDeviceToHost, m->stream));
+        MCK(cudaStreamSynchronize(m->stream));
+    }
+    return FFG_OK;
+}
+
 int ffg_mlp_selftest_gemm(ffg_mlp* m, int N, int K, const uint16_t* a, const uint16_t* b, float* d) {
     if (!m || !a || !b || !d) return FFG_ERR_ARG;
     if (K <= 0 || K > 128 || K % 16 || N < 16 || N > 256 || N % 16)
@@ -1092,10 +1189,10 @@ int ffg_mlp_selftest_gemm(ffg_mlp* m, int N, int K, const uint16_t* a, const uin
 
 int ffg_drop_features(ffg_ctx* ctx, const uint64_t* keys, size_t stride, const double* coef, const int32_t* gate,
                       size_t n, const ffg_pauli_gate* gates, size_t ngates, const int32_t* batch_of_gate,
-                      int32_t nbatches, const float* coords, int32_t obs_qubit, int32_t maxdegree, float* feat,
-                      uint16_t* x) {
+                      int32_t nbatches, const float* coords, int32_t obs_qubit, int32_t maxdegree,
+                      const float* shift, const float* scale, float* feat, uint16_t* x) {
     if (!ctx || (n && (!keys || !coef || !gate)) || !gates || !ngates || !batch_of_gate || nbatches < 1 || !coords ||
-        obs_qubit < 0 || obs_qubit >= 128)
+        obs_qubit < 0 || obs_qubit >= 128 || (!shift != !scale))
         return FFG_ERR_ARG;
     if (!n) return FFG_OK;
     cudaStream_t st = (cudaStream_t)ffg_stream(ctx);
@@ -1131,10 +1228,12 @@ int ffg_drop_features(ffg_ctx* ctx, const uint64_t* keys, size_t stride, const d
     };
     cudaError_t e = cudaMalloc(&dg, ngates * sizeof(FeatGate));
     if (e == cudaSuccess) e = cudaMalloc(&db, ngates * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&dc, 256 * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dc, 320 * 4);  // coords, then shift and scale
     if (e == cudaSuccess) e = cudaMemcpyAsync(dg, fg.data(), ngates * sizeof(FeatGate), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(db, batch_of_gate, ngates * 4, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dc, coords, 256 * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && shift) e = cudaMemcpyAsync(dc + 256, shift, 32 * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && scale) e = cudaMemcpyAsync(dc + 288, scale, 32 * 4, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
         FeatArgs A{};
         A.key = keys;
@@ -1153,6 +1252,8 @@ int ffg_drop_features(ffg_ctx* ctx, const uint64_t* keys, size_t stride, const d
         A.ly = ly;
         A.feat = feat;
         A.x = reinterpret_cast<__nv_bfloat16*>(x);
+        A.shift = shift ? dc + 256 : nullptr;
+        A.scale = scale ? dc + 288 : nullptr;
         drop_features_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(A);
         e = cudaGetLastError();
     }

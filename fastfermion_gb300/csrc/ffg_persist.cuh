@@ -40,7 +40,7 @@ struct PersistState {
     u64 bcast[4];     // Bcast record released by grid barriers (own 32-byte line)
 };
 
-constexpr long long kBarrierLimitCycles = 4000000000ll;  // about 2 s at 2 GHz
+constexpr long long kBarrierLimitCycles = 4000000000ll;  // default wait limit: about 2 s at 2 GHz
 constexpr int kPBlock = 512;                             // threads per block of the persistent kernel
 
 // Grid-wide barrier for a cooperative launch that also folds the op's delta
@@ -55,7 +55,8 @@ struct Bcast {
     u32 xapps;
 };
 
-__device__ __forceinline__ bool grid_sync_fold(PersistState* ps, Bcast* bc, int slot, Bcast* out) {
+__device__ __forceinline__ bool grid_sync_fold(PersistState* ps, Bcast* bc, int slot, Bcast* out,
+                                               long long limit) {
     __shared__ int ok;
     __shared__ Bcast sb;
     __syncthreads();
@@ -89,7 +90,7 @@ __device__ __forceinline__ bool grid_sync_fold(PersistState* ps, Bcast* bc, int 
                     ok = 0;
                     break;
                 }
-                if (clock64() - t0 > kBarrierLimitCycles) {
+                if (clock64() - t0 > limit) {
                     atomicExch(&ps->bar_timeout, 1u);
                     ok = 0;
                     break;
@@ -108,9 +109,9 @@ __device__ __forceinline__ bool grid_sync_fold(PersistState* ps, Bcast* bc, int 
 }
 
 // Plain grid barrier (used between the phases of a Clifford segment).
-__device__ __forceinline__ bool grid_sync(PersistState* ps, Bcast* bc) {
+__device__ __forceinline__ bool grid_sync(PersistState* ps, Bcast* bc, long long limit) {
     Bcast dummy;
-    return grid_sync_fold(ps, bc, 0, &dummy);
+    return grid_sync_fold(ps, bc, 0, &dummy, limit);
 }
 
 // --- one Pauli rotation over positions [0, n_in) (pair butterfly) ----------
@@ -414,6 +415,7 @@ struct PersistArgs {
     const GroupArgs<2>* groups2;
     int op_begin, op_end;
     int compact_min;  // stop for compaction when dead > alive and dead > compact_min
+    long long barrier_limit;  // clock cycles a block waits at a grid barrier before giving up
 };
 
 template <int KW, bool CPLX, bool PAULI, bool FUSE2>
@@ -507,9 +509,9 @@ __global__ void __launch_bounds__(kPBlock, 2) persistent_kernel(StoreView s, Dev
             pass_trunc<KW, CPLX, (PAULI ? NW : 0)>(s, t, n, d_alive);
         } else if (op.type == OP_CLIFF && PAULI) {
             pass_cliff_map<NW, CPLX>(s, pa.cliff + op.begin, op.end - op.begin, n);
-            if (!grid_sync(ps, bc)) { stop = 3; break; }
+            if (!grid_sync(ps, bc, pa.barrier_limit)) { stop = 3; break; }
             pass_clear_slots(s);
-            if (!grid_sync(ps, bc)) { stop = 3; break; }
+            if (!grid_sync(ps, bc, pa.barrier_limit)) { stop = 3; break; }
             pass_index<KW>(s, C, n);
         }
         const long long bd = block_sum_ll(d_alive, sh);
@@ -522,7 +524,7 @@ __global__ void __launch_bounds__(kPBlock, 2) persistent_kernel(StoreView s, Dev
         }
         stage(o + 1);  // prefetch the next op while waiting at the barrier
         Bcast f;
-        if (!grid_sync_fold(ps, bc, slot, &f)) {
+        if (!grid_sync_fold(ps, bc, slot, &f, pa.barrier_limit)) {
             stop = 3;
             break;
         }

@@ -26,8 +26,14 @@ Everything runs on the GPU through the C ABI:
 Plain propagation at W' is the judge of the held-out error and the fallback:
 ``Surrogate.estimate`` returns the corrected W value only when the validated
 held-out error is within the bound, and otherwise runs plain W'.  PyTorch
-serves only as device memory (tensors passed by address) and for shuffling
-rows between steps.
+serves only as device memory (tensors passed to the C ABI by address).
+
+Training objective.  With the coefficient threshold on, the labels of single
+partners do not add up to the W' value (a partner's descendants below tau are
+erased alone, while in the joint W' run they merge with others), so the
+network is trained on the set-level loss sum_theta (predicted correction -
+(judge - low))^2 over the training parameter values, optionally with the
+per-partner labels as a second term.
 """
 import math
 import time
@@ -147,124 +153,187 @@ class Workload:
 
 
 class Sample:
-    """Dropped partners of one parameter value: device BF16 features x [n][32],
-    device FP64 coefficients, and for training data the transfer targets and
-    the sum of the labels."""
+    """Dropped partners of one parameter value: the W value `low`, the FP32
+    features `feat` [n][32] and the device record of the drops (`drops`, kept
+    alive for the network's input and coefficients)."""
 
-    def __init__(self, theta, low, x, coef, n, keep=None, target=None, label_sum=None):
-        self.theta, self.low, self.x, self.coef, self.n = theta, low, x, coef, n
-        self.keep, self.target, self.label_sum = keep, target, label_sum
+    def __init__(self, theta, low, n, drops, feat, seconds):
+        self.theta, self.low, self.n, self.drops, self.feat, self.seconds = theta, low, n, drops, feat, seconds
+        self.x = None
+        self.judge = self.judge_seconds = self.labels = None
+
+    def coef(self):
+        """device address of the coefficients (FP64 [n])"""
+        return self.drops.device()[2]
+
+    def inputs(self, ctx, wl, shift, scale):
+        """BF16 network input [n][32] (standardised features)."""
+        import torch
+        self.x = torch.zeros((max(self.n, 1), 32), dtype=torch.int16, device="cuda")
+        if self.n:
+            tab, bog, nb = wl.table(self.theta)
+            dk, stride, dre, _, dg = self.drops.device()
+            _native.drop_features(ctx, dk, stride, dre, dg, self.n, tab, bog, nb, wl.coords, wl.obs_site,
+                                  wl.maxdegree, x=self.x, shift=shift, scale=scale)
+        return self.x
 
 
-def make_sample(ctx, wl, theta, with_labels=False):
-    """The W propagation at theta with capture, and the features (with_labels:
-    and the W' labels) of its dropped partners above tau."""
+def make_sample(ctx, wl, theta, features=True):
+    """The W propagation at theta recording its dropped partners above tau, and
+    their FP32 features."""
     import torch
     tab, bog, nb = wl.table(theta)
     k, re, im = wl.observable()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     res, drops = ctx.pauli_propagate_capture(k, re, im, tab, pauli_params(wl.maxdegree, wl.tau),
                                              capdeg=wl.maxdegree_hi, min_abs=wl.tau)
     low = res.overlapwithzero().real
     res.free()
     n = len(drops)
-    x = torch.zeros((max(n, 1), 32), dtype=torch.int16, device="cuda")
-    if not with_labels:
+    feat = None
+    if features:
+        feat = torch.zeros((max(n, 1), 32), dtype=torch.float32, device="cuda")
         if n:
             dk, stride, dre, _, dg = drops.device()
-            _native.drop_features(ctx, dk, stride, dre, dg, n, tab, bog, nb, wl.coords, wl.obs_site,
-                                  wl.maxdegree, None, x)
-            return Sample(theta, low, x, dre, n, keep=drops)
-        drops.free()
-        return Sample(theta, low, x, None, 0)
-    hk, hre, _, hg = drops.copy()
-    drops.free()
-    lab = labels(ctx, tab, hk, hre, hg, wl.maxdegree_hi, wl.tau) if n else np.zeros(0)
-    coef = torch.from_numpy(hre.copy()).cuda()
-    if n:
-        kd = torch.from_numpy(hk.view(np.int64).copy()).cuda()
-        gd = torch.from_numpy(hg.copy()).cuda()
-        _native.drop_features(ctx, kd, n, coef, gd, n, tab, bog, nb, wl.coords, wl.obs_site, wl.maxdegree,
-                              None, x)
-    target = torch.from_numpy((lab / np.where(hre == 0, 1.0, hre)).astype(np.float32)).cuda()
-    return Sample(theta, low, x, coef, n, target=target, label_sum=float(lab.sum()))
+            _native.drop_features(ctx, dk, stride, dre, dg, n, tab, bog, nb, wl.coords, wl.obs_site, wl.maxdegree,
+                                  feat=feat)
+    torch.cuda.synchronize()
+    return Sample(theta, low, n, drops, feat, time.perf_counter() - t0)
+
+
+def _f64(addr, n):
+    """device FP64 [n] at addr, copied into a torch tensor"""
+    import torch
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    _native.device_copy(out.data_ptr(), addr, 8 * n)
+    return out
 
 
 class Surrogate:
-    """The trained network, its training history and its validated error."""
+    """The network, trained on the corrections judge(theta) - low(theta) of a set
+    of training parameter values (and, optionally, on per-partner labels), and
+    validated on held-out values."""
 
     def __init__(self, ctx, wl, seed=0):
-        self.ctx, self.wl = ctx, wl
+        self.ctx, self.wl, self.seed = ctx, wl, seed
         self.mlp = _native.MLP(ctx)
         self.mlp.set_params(init_params(seed))
-        self.seed = seed
+        self.shift = self.scale = None
         self.held_out_error = math.inf
+        self.bound = 1e-3
         self.history = []
 
-    def train(self, samples, steps=2000, batch=8192, lr=1e-3, lr_end=1e-5):
-        """Adam on the coefficient-weighted squared error of the predicted
-        contributions, sum_r c_r^2 (t_pred - t_r)^2 / sum_r c_r^2 over each
-        minibatch; cosine learning-rate decay from lr to lr_end."""
+    def collect(self, thetas, labels_for=()):
+        """A Sample per theta with the judge's value (plain W', timed) and, for
+        thetas in labels_for, the W' labels of its dropped partners (in the
+        device order of the record)."""
         import torch
-        xs = torch.cat([s.x[:s.n] for s in samples if s.n])
-        ts = torch.cat([s.target[:s.n] for s in samples if s.n])
-        cs = torch.cat([s.coef[:s.n] for s in samples if s.n])
-        w_all = (cs * cs).float()
-        n = xs.shape[0]
-        g = torch.Generator(device="cuda")
-        g.manual_seed(self.seed)
-        b = min(batch, n)
+        data = []
+        for th in thetas:
+            s = make_sample(self.ctx, self.wl, th)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.judge = self.wl.plain(self.ctx, th)
+            torch.cuda.synchronize()
+            s.judge_seconds = time.perf_counter() - t0
+            if th in labels_for and s.n:
+                dk, stride, dre, _, dg = s.drops.device()
+                hk = np.stack([_native.device_view(dk + 8 * w * stride, (s.n,), "<u8").cpu().numpy()
+                               for w in range(4)])
+                hre = _native.device_view(dre, (s.n,), "<f8").cpu().numpy()
+                hg = _native.device_view(dg, (s.n,), "<i4").cpu().numpy()
+                s.labels = labels(self.ctx, self.wl.table(th)[0], hk, hre, hg, self.wl.maxdegree_hi, self.wl.tau)
+            data.append(s)
+        return data
+
+    def fit(self, data, steps=6000, lr=3e-3, label_weight=0.0):
+        """Adam on the set-level loss L = sum_theta (sum_D c_D t(x_D) - (judge -
+        low))^2 (ffg_mlp_set_targets) plus label_weight times the normalised
+        coefficient-weighted squared error of the transfers of partners with
+        labels; the features are standardised with the training set's mean and
+        deviation; constant rate for the first half of the steps, cosine decay
+        to 1% in the second."""
+        import torch
+        live = [s for s in data if s.n]
+        feats = torch.cat([s.feat[:s.n] for s in live])
+        self.shift = feats.mean(0).cpu().numpy().astype(np.float32)
+        self.scale = (1.0 / (feats.std(0) + 1e-3)).cpu().numpy().astype(np.float32)
+        X = torch.cat([s.inputs(self.ctx, self.wl, self.shift, self.scale)[:s.n] for s in live]).contiguous()
+        C = torch.cat([_f64(s.coef(), s.n) for s in live]).contiguous()
+        seg = torch.tensor(np.cumsum([0] + [s.n for s in live]), dtype=torch.int64, device="cuda")
+        delta = torch.tensor([s.judge - s.low for s in live], dtype=torch.float64, device="cuda")
+        n, ns = X.shape[0], len(live)
+        lab = lw = None
+        if label_weight > 0 and any(s.labels is not None for s in live):
+            c_h = C.cpu().numpy()
+            lab_h, lw_h, pos = [], [], 0
+            for s in live:
+                c = c_h[pos:pos + s.n]
+                pos += s.n
+                if s.labels is None:
+                    lab_h.append(np.zeros(s.n))
+                    lw_h.append(np.zeros(s.n))
+                else:
+                    lab_h.append(s.labels / np.where(c == 0, 1.0, c))
+                    lw_h.append(c * c)
+            lw_all = np.concatenate(lw_h)
+            lw_all *= label_weight / max(lw_all.sum(), 1e-300)
+            lab = torch.from_numpy(np.concatenate(lab_h).astype(np.float32)).cuda()
+            lw = torch.from_numpy(lw_all.astype(np.float32)).cuda()
+        T = torch.empty(n, dtype=torch.float32, device="cuda")
+        W = torch.empty(n, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        perm = torch.randperm(n, device="cuda", generator=g)
-        pos = 0
-        for step in range(steps):
-            if pos + b > n:
-                perm = torch.randperm(n, device="cuda", generator=g)
-                pos = 0
-            idx = perm[pos:pos + b]
-            pos += b
-            x = xs[idx].contiguous()
-            t = ts[idx].contiguous()
-            w = w_all[idx]
-            w = (w / w.sum()).contiguous()
-            rate = lr_end + 0.5 * (lr - lr_end) * (1 + math.cos(math.pi * step / max(steps - 1, 1)))
-            loss = self.mlp.adam_step(x, t, w, b, rate, want_loss=(step % 200 == 0 or step == steps - 1))
-            if loss is not None:
-                self.history.append((step, loss))
+        half = steps // 2
+        for it in range(steps):
+            rate = lr if it < half else lr * (0.01 + 0.5 * (1 + math.cos(math.pi * (it - half) / max(steps - half, 1))))
+            want = it % 1000 == 0 or it == steps - 1
+            loss = self.mlp.set_targets(X, n, C, seg, delta, ns, T, W, lab, lw, want_loss=want)
+            self.mlp.adam_step(X, T, W, n, rate)
+            if want:
+                self.history.append((it, loss[0], loss[1]))
         torch.cuda.synchronize()
         self.train_seconds = time.perf_counter() - t0
-        self.rows = n
+        self.rows, self.sets, self.steps = n, ns, steps
         return self
 
     def correction(self, sample):
-        """sum over the sample's dropped partners of c * t_pred (device work)."""
+        """sum over the sample's dropped partners of c * t(x), on the GPU."""
         import torch
         if not sample.n:
             return 0.0
+        x = sample.inputs(self.ctx, self.wl, self.shift, self.scale)
         t = torch.empty(sample.n, dtype=torch.float32, device="cuda")
-        coef = sample.coef if isinstance(sample.coef, int) else sample.coef
-        return self.mlp.correction(sample.x, coef, sample.n, t)
+        return self.mlp.correction(x, sample.coef(), sample.n, t)
 
-    def validate(self, held_out, judge_values, bound=1e-3):
-        """Held-out |corrected - judge| for each sample; records the largest."""
-        errs = []
-        for s, j in zip(held_out, judge_values):
-            errs.append(abs(s.low + self.correction(s) - j))
-        self.held_out_error = max(errs) if errs else math.inf
-        self.bound = bound
-        return np.array(errs)
+    def predict(self, theta):
+        """(corrected W value, seconds of W propagation with capture + features
+        + network, plain W value)"""
+        import torch
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s = make_sample(self.ctx, self.wl, theta, features=False)
+        v = s.low + self.correction(s)
+        torch.cuda.synchronize()
+        return v, time.perf_counter() - t0, s.low
+
+    def validate(self, held):
+        """Held-out errors |corrected - judge|; records the largest as the
+        validated error that decides between the surrogate and the fallback."""
+        errs = np.array([abs(s.low + self.correction(s) - s.judge) for s in held])
+        self.held_out_error = float(errs.max()) if errs.size else math.inf
+        return errs
 
     def estimate(self, theta):
         """(value, seconds, path): the corrected W estimate when the validated
         held-out error is within the bound, else the plain W' propagation."""
+        if self.held_out_error <= self.bound:
+            v, sec, _ = self.predict(theta)
+            return v, sec, "surrogate"
         import torch
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        if self.held_out_error <= getattr(self, "bound", 1e-3):
-            s = make_sample(self.ctx, self.wl, theta)
-            v = s.low + self.correction(s)
-            path = "surrogate"
-        else:
-            v = self.wl.plain(self.ctx, theta)
-            path = "fallback"
+        v = self.wl.plain(self.ctx, theta)
         torch.cuda.synchronize()
-        return v, time.perf_counter() - t0, path
+        return v, time.perf_counter() - t0, "fallback"

@@ -150,6 +150,10 @@ void* ffg_stream(const ffg_ctx* ctx);
  *   store_headroom    orbit windows size their output stores for this many times
  *                     the entering terms, 1..64 (4); a batch that outgrows its
  *                     store runs again after the store grows
+ *   barrier_limit_kcycles  thousands of clock cycles a block of the persistent
+ *                     kernel waits at a grid barrier before the launch gives up
+ *                     and the call returns FFG_ERR_STATE, 1..4000000 (4000000,
+ *                     about 2 s); the context stays usable
  *   group_region_cap  members of the first global-memory region of a group too
  *                     large for shared memory, a power of two >= 64 (16384; the
  *                     Majorana path starts at a quarter); regions grow x4 on
@@ -338,6 +342,19 @@ int ffg_mlp_adam_step(ffg_mlp* m, const uint16_t* x, const float* target, const 
 /* Predicted correction sum_r coef[r] t[r] (coef device FP64 [n]); t receives
  * the n transfers. */
 int ffg_mlp_correction(ffg_mlp* m, const uint16_t* x, const double* coef, size_t n, float* t, double* out);
+/* Set-level targets: rows seg[s] .. seg[s+1] (device int64 [nseg+1], seg[0] =
+ * 0, seg[nseg] = n) are the dropped partners of one circuit, whose total
+ * correction should be delta[s] (device FP64 [nseg]).  Writes device target and
+ * weight [n] such that one ffg_mlp_adam_step on (x, target, weight) is a step
+ * on
+ *   L = sum_s (sum_{r in s} coef_r y_r - delta_s)^2
+ *       + sum_r label_weight_r (y_r - label_r)^2
+ * (label / label_weight: device FP32 [n], or both NULL for the first term
+ * alone); loss (host [2], may be NULL) receives the two terms at the current
+ * parameters. */
+int ffg_mlp_set_targets(ffg_mlp* m, const uint16_t* x, size_t n, const double* coef, const int64_t* seg,
+                        const double* delta, size_t nseg, const float* label, const float* label_weight,
+                        float* target, float* weight, double* loss);
 /* Self-test of the tensor-core path: D[128][N] = A[128][K] B[N][K]^T with host
  * BF16 A, B and FP32 D (K in 16..128, N in 16..256, multiples of 16). */
 int ffg_mlp_selftest_gemm(ffg_mlp* m, int N, int K, const uint16_t* a, const uint16_t* b, float* d);
@@ -346,12 +363,13 @@ int ffg_mlp_selftest_gemm(ffg_mlp* m, int N, int K, const uint16_t* a, const uin
  * (host, [ngates]) is the commuting run of each gate in application order
  * (nbatches runs), coords (host, [2][128]) the lattice coordinates of the
  * qubits, obs_qubit the observable's site, maxdegree the cutoff that dropped
- * them.  Writes FP32 features feat[n][32] and/or BF16 x[n][32] (device, either
- * may be NULL). */
+ * them.  Writes FP32 features feat[n][32] and/or the BF16 network input
+ * x[n][32] = (feature - shift) * scale (device, either may be NULL; shift and
+ * scale are host [32] arrays, both NULL for no standardisation). */
 int ffg_drop_features(ffg_ctx* ctx, const uint64_t* keys, size_t stride, const double* coef, const int32_t* gate,
                       size_t n, const ffg_pauli_gate* gates, size_t ngates, const int32_t* batch_of_gate,
-                      int32_t nbatches, const float* coords, int32_t obs_qubit, int32_t maxdegree, float* feat,
-                      uint16_t* x);
+                      int32_t nbatches, const float* coords, int32_t obs_qubit, int32_t maxdegree,
+                      const float* shift, const float* scale, float* feat, uint16_t* x);
 
 /* -------------------------------------------------------------------------- */
 /* Allocation-free rotations.  No counterpart in the reference: this entry

@@ -215,3 +215,25 @@ def features(keys, coef, gate, gates, batch_of_gate, nbatches, coords, obs, maxd
         f[30] = (cx - ox) / lx
         f[31] = (cy - oy) / ly
     return out
+
+
+def set_targets(y, coef, seg, delta, label=None, label_weight=None):
+    """Per-row targets and weights whose weighted squared error has the gradient
+    of the set-level loss (ffg_mlp_set_targets): returns (target, weight,
+    set loss, label loss)."""
+    y = np.asarray(y, np.float64)
+    coef = np.asarray(coef, np.float64)
+    seg = np.asarray(seg, np.int64)
+    n, ns = y.size, seg.size - 1
+    R = np.array([np.dot(coef[seg[s]:seg[s + 1]], y[seg[s]:seg[s + 1]]) - delta[s] for s in range(ns)])
+    segid = np.repeat(np.arange(ns), np.diff(seg))
+    g = R[segid] * coef
+    w = np.full(n, np.float32(1.0 / n), dtype=np.float64)
+    lab_loss = 0.0
+    if label is not None:
+        e = y - np.asarray(label, np.float64)
+        lw = np.asarray(label_weight, np.float64)
+        g = g + lw * e
+        w = w + lw
+        lab_loss = float(np.sum(lw * e * e))
+    return y - g / w, w, float(np.sum(R * R)), lab_loss

@@ -226,3 +226,46 @@ def test_gpu_labels_account_for_the_truncation_error():
     f_low, f_high = low.overlapwithzero().real, high.overlapwithzero().real
     assert abs(f_high - f_low) > 1e-3
     assert abs(f_high - (f_low + lab.sum())) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_barrier_timeout_reports_an_error_and_the_context_recovers():
+    """Failure detection without a fault: with a 1000-cycle limit the blocks of
+    the persistent kernel give up at a grid barrier; the call returns
+    FFG_ERR_STATE instead of hanging, and the same context then propagates
+    correctly with the default limit."""
+    tab = ff.encode_pauli_circuit(ff.build_circuit(ff.workloads.chain_circuit()))
+    k, re, im = _z(7)
+    ctx = _native.context(0)
+    p = dict(_gpu_params(6, 1e-8), batched=0)  # unbatched: one persistent launch runs the rotations
+    old = ctx.get_option("barrier_limit_kcycles")
+    try:
+        ctx.set_option("barrier_limit_kcycles", 1)
+        with pytest.raises(_native.FFGError, match="grid barrier timed out"):
+            ctx.pauli_propagate(k, re, im, tab, p)
+    finally:
+        ctx.set_option("barrier_limit_kcycles", old)
+    r = ctx.pauli_propagate(k, re, im, tab, p)
+    o = O.pauli_propagate(tab, k, re, im, maxdegree=6, mincoeff=1e-8, batched=False)
+    assert_same_terms(r.copy(), (o.keys, o.re, o.im))
+
+
+@pytest.mark.gpu
+def test_gpu_group_regions_grow_and_groups_run_again():
+    """Groups too large for shared memory start in 64-member global-memory
+    regions (option group_region_cap), outgrow them and run again in regions
+    four times larger; the term set is unchanged (10x10 kicked Ising, W=8,
+    theta_h=0.5, against the reference fixture)."""
+    from golden_io import load
+    fx = load("cfg2_kicked_ising_0p5000")
+    ctx = _native.context(0)
+    p = _gpu_params(int(fx["maxdegree"]), float(fx["mincoeff"]))
+    old = ctx.get_option("group_region_cap")
+    try:
+        ctx.set_option("group_region_cap", 64)
+        r = ctx.pauli_propagate(fx["obs_keys"], fx["obs_re"], fx["obs_im"], fx["gates"], p)
+        prof = ctx.profile()
+    finally:
+        ctx.set_option("group_region_cap", old)
+    assert prof["orbit_max_group"] > 4096, prof["orbit_max_group"]  # some group used the global regions
+    assert_same_terms(r.copy(), (fx["res_keys"], fx["res_re"], fx["res_im"]))

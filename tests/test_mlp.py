@@ -169,3 +169,45 @@ def test_drop_features_match_restatement():
     err = np.abs(got - want) / np.maximum(np.abs(want), 1.0)
     assert np.max(err) <= 1e-6, (np.argmax(np.max(err, axis=0)), np.max(err, axis=0))
     assert np.array_equal(x.cpu().numpy().view(np.uint16), R.bf16_bits(got))
+    # standardised network input: bf16((f - shift) * scale) in FP32
+    shift = want.mean(0).astype(np.float32)
+    scale = (1.0 / (want.std(0) + 1e-3)).astype(np.float32)
+    _native.drop_features(ctx, kd, n, _dev(torch, dre), _dev(torch, dg), n, tab, bog, nb, coords, 55, 6, None, x,
+                          shift=shift, scale=scale)
+    std = ((got - shift) * scale).astype(np.float32)
+    assert np.array_equal(x.cpu().numpy().view(np.uint16), R.bf16_bits(std))
+
+
+@pytest.mark.gpu
+def test_set_targets_match_restatement_and_fit_set_totals(mlp):
+    """Set-level training: the targets/weights written on the GPU against the
+    restatement, and Adam steps on them drive every segment's total
+    sum_r c_r y_r to its target."""
+    import torch
+    rng = np.random.default_rng(5)
+    nseg, per = 12, 300
+    n = nseg * per
+    p, xb, _, _ = _problem(21, n)
+    mlp.set_params(p)
+    seg = np.arange(0, n + 1, per, dtype=np.int64)
+    coef = rng.normal(size=n) * 10 ** rng.uniform(-4, -1, size=n)
+    delta = rng.normal(scale=0.05, size=nseg)
+    label = rng.normal(size=n).astype(np.float32)
+    lw = (coef * coef / np.sum(coef * coef) * 0.1).astype(np.float32)
+    x = _dev(torch, xb.view(np.int16))
+    dc, ds, dd = _dev(torch, coef), _dev(torch, seg), _dev(torch, delta)
+    dl, dlw = _dev(torch, label), _dev(torch, lw)
+    t = torch.zeros(n, dtype=torch.float32, device="cuda")
+    w = torch.zeros(n, dtype=torch.float32, device="cuda")
+    l_set, l_lab = mlp.set_targets(x, n, dc, ds, dd, nseg, t, w, dl, dlw, want_loss=True)
+    y = torch.zeros(n, dtype=torch.float32, device="cuda")
+    mlp.forward(x, n, y)
+    wt, ww, ws, wl = R.set_targets(y.cpu().numpy(), coef, seg, delta, label, lw)
+    assert np.allclose(w.cpu().numpy(), ww, rtol=1e-6)
+    assert np.allclose(t.cpu().numpy(), wt, rtol=1e-5, atol=1e-5 * np.max(np.abs(wt)))
+    assert l_set == pytest.approx(ws, rel=1e-9) and l_lab == pytest.approx(wl, rel=1e-5)
+    for _ in range(300):
+        mlp.set_targets(x, n, dc, ds, dd, nseg, t, w)
+        mlp.adam_step(x, t, w, n, lr=3e-4)
+    l_end, _ = mlp.set_targets(x, n, dc, ds, dd, nseg, t, w, want_loss=True)
+    assert l_end < 1e-2 * l_set, (l_set, l_end)
