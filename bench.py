@@ -267,8 +267,30 @@ class BatchedAnsatz:
                 "checkpoint_every": 1}
 
 
+class LearnedCorrection:
+    """Learned truncation correction on the 10x10 kicked-Ising circuit (20 steps,
+    observable Z_55, threshold 1e-6): plain W=6 propagation plus the surrogate's
+    correction, judged against plain W'=10.  Training: 64 seeded theta_h values
+    in [0.05, pi/2]; evaluation: 16 held-out values from the same range.  The
+    line's value is the time to reach |delta<O>| <= 1e-3 on the 16 held-out
+    values (seconds, summed): the surrogate path (W=6 with capture, features,
+    network; plus the W'=10 fallback where its error exceeds the bound),
+    against the cheapest plain propagation within the bound."""
+    name = "learned_correction_kicked_ising_10x10_w6_to_w10"
+    metric = ("time-to-|delta<O>|<=1e-3 on 16 held-out theta_h (s), surrogate-corrected W=6 "
+              "(fallback to plain W=10 where it misses) vs plain")
+    kind = "surrogate"
+    members, steps, lr = 2, 20000, 3e-3
+
+    def config(self):
+        return {"workload": self.name, "lattice": "10x10 open", "trotter_steps": 20, "maxdegree": 6,
+                "judge_maxdegree": 10, "mincoeff": 1e-6, "observable": "Z_55", "train_theta_h": 64,
+                "held_out_theta_h": 16, "network": "32-128-128-128-1 GELU, BF16 tcgen05 GEMMs, FP32 accumulation",
+                "ensemble": self.members, "train_steps": self.steps}
+
+
 WORKLOADS = {"kicked_ising": KickedIsing, "kicked_ising_w10": KickedIsingW10, "hubbard": Hubbard,
-             "hea": BatchedAnsatz}
+             "surrogate": LearnedCorrection, "hea": BatchedAnsatz}
 
 
 def parse():
@@ -421,9 +443,14 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    wl = args.wl
+    if wl.kind == "surrogate":
+        print(json.dumps({"impl": "reference", "unavailable": (
+            "the reference reaches 1e-3 only by plain W=10, hours on the host for the 16 held-out theta_h "
+            "(986 s at theta_h=0.3 alone); a bounded sample of it is the cpu_baseline of the GPU line")}))
+        return 0
     from oracle import oracle as O
     O.build()
-    wl = args.wl
     tabs = wl.tables()
     cores = os.cpu_count() or 1
     ref = reference_module() if hasattr(wl, "ref_sample") else None
@@ -530,6 +557,116 @@ def main_batched(args, rank, ws, local, dist):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+# ---------------------------------------------------------------------------
+# learned correction (time to accuracy)
+# ---------------------------------------------------------------------------
+MLP_FLOPS_PER_ROW = 2 * (32 * 128 + 2 * 128 * 128 + 128)
+
+
+def mlp_roofline(ctx, mlp, rows=1 << 21, reps=10):
+    """Achieved TFLOP/s of the network's forward kernel (mlp_forward_kernel) on
+    `rows` synthetic BF16 inputs, CUDA events on the context's stream."""
+    import torch
+    x = (torch.randn(rows, 32, device="cuda") * 0.5).to(torch.bfloat16).view(torch.int16)
+    y = torch.empty(rows, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(3):
+        mlp.forward(x, rows, y)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        mlp.forward(x, rows, y)
+    e1.record(stream)
+    e1.synchronize()
+    sec = e0.elapsed_time(e1) * 1e-3 / reps
+    return MLP_FLOPS_PER_ROW * rows / sec / 1e12, sec
+
+
+def main_surrogate(args, rank, ws, local, dist):
+    import torch
+
+    from fastfermion_gb300 import _native, surrogate as S, workloads as W
+    torch.cuda.set_device(local)
+    ctx = _native.context(local)
+    wl = S.kicked_ising_workload()
+    train, held = W.learned_correction_thetas()
+    t0 = time.perf_counter()
+    sur = S.Surrogate(ctx, wl, seed=0, members=args.wl.members)
+    data = sur.collect(train)
+    t_data = time.perf_counter() - t0
+    sur.fit(data, steps=args.wl.steps, lr=args.wl.lr)
+    hdata = sur.collect(held)
+    errs = sur.validate(hdata)
+    for _ in range(args.warmup):
+        sur.predict(held[0])
+    with ClockSampler(local) as clk:
+        rows = S.evaluate(sur, hdata)
+        reps = []
+        for _ in range(max(args.steps - 1, 0)):  # more timings of the prediction path
+            reps.append([sur.predict(s.theta)[1] for s in hdata])
+    t_pred = np.median(np.array([[r["t_predict"] for r in rows]] + reps), axis=0)
+    # kernels of one query: the capture propagation's, the feature kernel, and a
+    # forward pass and a reduction per ensemble member
+    sur.predict(held[0])
+    launches = sum(ctx.profile()["kernel_launches"] + 1 + 2 * args.wl.members for _ in rows)
+    h2d = sum(wl.table(s.theta)[0].nbytes + 48 for s in hdata)  # gate table + observable per query
+    d2h = 16 * len(hdata)  # the value and the record size
+    t_sur = sum(tp + (r["t_judge"] if r["err_surrogate"] > 1e-3 else 0.0) for tp, r in zip(t_pred, rows))
+    t_plain = sum(r["t_plain"] for r in rows)
+    tflops, t_fwd = mlp_roofline(ctx, sur.mlp)
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    peak = peaks.get("bf16_tflops", 1900.0)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        ref = reference_module()
+        sub = sorted(hdata, key=lambda s: s.judge_seconds)[:4]  # the quickest judge runs
+        if ref is not None:
+            from fastfermion_gb300 import workloads as WL
+            obs = ref.poly(f"Z{OBS_SITE}")
+            tr = 0.0
+            for s in sub:
+                circ = [ref.ROT(g[1], list(g[2]), g[3]) for g in WL.kicked_ising_circuit(s.theta)]
+                a = time.perf_counter()
+                ref.propagate(circ, obs, n_threads=os.cpu_count(), maxdegree=10, mincoeff=1e-6, parallel="sharded")
+                tr += time.perf_counter() - a
+            cpu = {"value": tr, "unit": "s", "cores": os.cpu_count(), "kind": "reference",
+                   "sample": "plain W=10 (the only plain cutoff within 1e-3 where W=6 misses) on the 4 held-out theta_h "
+                             f"with the quickest GPU judge runs ({', '.join(f'{s.theta:.3f}' for s in sub)}); the GPU "
+                             f"judge takes {sum(s.judge_seconds for s in sub):.3f} s on them"}
+    if rank == 0:
+        within = int(sum(r["err_surrogate"] <= 1e-3 for r in rows))
+        within_plain = int(sum(r["err_plain_w"] <= 1e-3 for r in rows))
+        out = {
+            "metric": args.wl.metric, "value": t_sur, "unit": "s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_sur, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 network, f64 propagation", "data": "synthetic",
+            "config": dict(args.wl.config(), plain_seconds=t_plain, speedup_vs_plain=t_plain / t_sur,
+                           held_out_within_1e3_surrogate=within, held_out_within_1e3_plain_w6=within_plain,
+                           held_out_max_error=float(errs.max()), validated_path="surrogate" if
+                           sur.held_out_error <= 1e-3 else "fallback (validated error above 1e-3)",
+                           data_seconds=t_data, train_seconds=sur.train_seconds, train_rows=sur.rows,
+                           per_theta=[{k: (round(v, 6) if isinstance(v, float) else v) for k, v in r.items()}
+                                      for r in rows], l2="not flushed (per-query latency)"),
+            "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
+                         "frac": tflops / peak, "traffic": None,
+                         "kernel": "mlp_forward_kernel (3 tcgen05 BF16 GEMMs per 128-row tile)",
+                         "launch_unit": "forward pass over 2^21 synthetic rows",
+                         "algorithmic_flops": f"{MLP_FLOPS_PER_ROW} per row", "launch_seconds": t_fwd,
+                         "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)" if peaks else "fallback"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": t_sur, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "note": "every timed query starts from host arrays and returns the value to the host"},
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+        }
+        print(json.dumps(out))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -537,6 +674,8 @@ def main():
     rank, ws, local, dist = dist_init()
     if args.wl.kind == "batched":
         return main_batched(args, rank, ws, local, dist)
+    if args.wl.kind == "surrogate":
+        return main_surrogate(args, rank, ws, local, dist)
     import torch
 
     import fastfermion_gb300 as ff  # noqa: F401

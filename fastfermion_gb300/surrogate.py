@@ -152,6 +152,21 @@ class Workload:
         return v
 
 
+def kicked_ising_workload():
+    """The learned-correction workload: the 10x10 kicked-Ising circuit (20
+    steps, RZZ(-pi/2) on the 180 edges then RX(theta_h) on every site),
+    observable Z at site (5,5), plain cutoff W=6 corrected towards the W'=10
+    judge, threshold 1e-6."""
+    from . import workloads as W
+    from .propagation import encode_pauli_circuit
+
+    def make(theta):
+        from . import build_circuit
+        return encode_pauli_circuit(build_circuit(W.kicked_ising_circuit(theta)))
+
+    return Workload(make, 10, 10, 55, 6, 10, 1e-6)
+
+
 class Sample:
     """Dropped partners of one parameter value: the W value `low`, the FP32
     features `feat` [n][32] and the device record of the drops (`drops`, kept
@@ -215,10 +230,14 @@ class Surrogate:
     of training parameter values (and, optionally, on per-partner labels), and
     validated on held-out values."""
 
-    def __init__(self, ctx, wl, seed=0):
+    def __init__(self, ctx, wl, seed=0, members=1):
         self.ctx, self.wl, self.seed = ctx, wl, seed
-        self.mlp = _native.MLP(ctx)
-        self.mlp.set_params(init_params(seed))
+        # an ensemble of `members` networks (seeds seed, seed+1, ...); the
+        # correction is their mean
+        self.mlps = [_native.MLP(ctx) for _ in range(members)]
+        for i, m in enumerate(self.mlps):
+            m.set_params(init_params(seed + i))
+        self.mlp = self.mlps[0]
         self.shift = self.scale = None
         self.held_out_error = math.inf
         self.bound = 1e-3
@@ -286,13 +305,15 @@ class Surrogate:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         half = steps // 2
-        for it in range(steps):
-            rate = lr if it < half else lr * (0.01 + 0.5 * (1 + math.cos(math.pi * (it - half) / max(steps - half, 1))))
-            want = it % 1000 == 0 or it == steps - 1
-            loss = self.mlp.set_targets(X, n, C, seg, delta, ns, T, W, lab, lw, want_loss=want)
-            self.mlp.adam_step(X, T, W, n, rate)
-            if want:
-                self.history.append((it, loss[0], loss[1]))
+        for k, mlp in enumerate(self.mlps):
+            for it in range(steps):
+                rate = lr if it < half else lr * (0.01 + 0.5 * (1 + math.cos(math.pi * (it - half) /
+                                                                           max(steps - half, 1))))
+                want = it % 1000 == 0 or it == steps - 1
+                loss = mlp.set_targets(X, n, C, seg, delta, ns, T, W, lab, lw, want_loss=want)
+                mlp.adam_step(X, T, W, n, rate)
+                if want:
+                    self.history.append((k, it, loss[0], loss[1]))
         torch.cuda.synchronize()
         self.train_seconds = time.perf_counter() - t0
         self.rows, self.sets, self.steps = n, ns, steps
@@ -305,7 +326,7 @@ class Surrogate:
             return 0.0
         x = sample.inputs(self.ctx, self.wl, self.shift, self.scale)
         t = torch.empty(sample.n, dtype=torch.float32, device="cuda")
-        return self.mlp.correction(x, sample.coef(), sample.n, t)
+        return sum(m.correction(x, sample.coef(), sample.n, t) for m in self.mlps) / len(self.mlps)
 
     def predict(self, theta):
         """(corrected W value, seconds of W propagation with capture + features
@@ -337,3 +358,31 @@ class Surrogate:
         v = self.wl.plain(self.ctx, theta)
         torch.cuda.synchronize()
         return v, time.perf_counter() - t0, "fallback"
+
+
+def evaluate(sur, held, bound=1e-3, plain_cutoffs=(6, 7, 8, 9)):
+    """Per held-out value: the error of the plain W value and of the corrected
+    one against the judge, the time of the surrogate path (prediction, plus
+    the fallback's W' run when the prediction misses the bound), and the time of
+    the cheapest plain run within the bound (a cutoff from plain_cutoffs, else
+    the judge's W' run)."""
+    import torch
+    rows = []
+    for s in held:
+        v, t_pred, low = sur.predict(s.theta)
+        err = abs(v - s.judge)
+        t_sur = t_pred + (s.judge_seconds if err > bound else 0.0)
+        t_plain, w_plain = s.judge_seconds, sur.wl.maxdegree_hi
+        for w in plain_cutoffs:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pv = sur.wl.plain(sur.ctx, s.theta, w)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            if abs(pv - s.judge) <= bound:
+                t_plain, w_plain = dt, w
+                break
+        rows.append(dict(theta=s.theta, judge=s.judge, low=low, corrected=v, err_plain_w=abs(low - s.judge),
+                         err_surrogate=err, t_predict=t_pred, t_surrogate=t_sur, t_plain=t_plain, w_plain=w_plain,
+                         t_judge=s.judge_seconds, n_drops=s.n))
+    return rows

@@ -254,10 +254,11 @@ def test_gpu_barrier_timeout_reports_an_error_and_the_context_recovers():
 def test_gpu_group_regions_grow_and_groups_run_again():
     """Groups too large for shared memory start in 64-member global-memory
     regions (option group_region_cap), outgrow them and run again in regions
-    four times larger; the term set is unchanged (10x10 kicked Ising, W=8,
-    theta_h=0.5, against the reference fixture)."""
+    four times larger; the term set is unchanged (10x10 kicked Ising, W=10,
+    theta_h=0.3, whose largest groups exceed the 4096-member shared-memory
+    tier, against the reference's own result)."""
     from golden_io import load
-    fx = load("cfg2_kicked_ising_0p5000")
+    fx = load("cfg2w10_kicked_ising_0p3000")
     ctx = _native.context(0)
     p = _gpu_params(int(fx["maxdegree"]), float(fx["mincoeff"]))
     old = ctx.get_option("group_region_cap")

@@ -73,7 +73,8 @@ circ = read_circuit("EXAMPLES/data/su4circuit-16.txt")
 obs = ff.poly("Z15")
 g = ffcore_gpu.propagate(circ, obs, maxdegree=4)
 c = ff.propagate(circ, obs, maxdegree=4)
-same = len(g.terms) == len(c.terms) and all(g.terms.get(k) == v for k, v in c.terms.items())
+gt, ct = g.terms, c.terms  # each .terms access builds a dict of every term
+same = len(gt) == len(ct) and all(gt.get(k) == v for k, v in ct.items())
 print(json.dumps({"n": len(g.terms), "o": g.overlapwithzero().real, "same": same}))
 '''.replace("EXAMPLES", os.path.join(STAGE, "_src", "examples"))
     with tempfile.TemporaryDirectory() as d:
