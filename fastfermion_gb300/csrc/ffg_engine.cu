@@ -882,19 +882,30 @@ struct Engine {
         const size_t tb = block_table_bytes<KW, CPLX>();
         const size_t tt = block_table_bytes<KW, CPLX, kTeamCap>();
         // the tier kernels at each thread count (options orbit_team_threads, orbit_block_threads)
-        auto team_k = ctx->orbit_team_threads == 128 ? orbit_process_big<NWo, CPLX, true, 128, kTeamCap>
-                                                     : orbit_process_big<NWo, CPLX, true, 256, kTeamCap>;
-        auto block_k = ctx->orbit_block_threads == 512 ? orbit_process_big<NWo, CPLX, true, 512, kBlockCap>
-                                                       : orbit_process_big<NWo, CPLX, true, 1024, kBlockCap>;
+        const bool rec = ctx->capture.n != nullptr;  // capture runs record the dropped partners
+        auto team_k = ctx->orbit_team_threads == 128
+                          ? (rec ? orbit_process_big<NWo, CPLX, true, 128, kTeamCap, true>
+                                 : orbit_process_big<NWo, CPLX, true, 128, kTeamCap>)
+                          : (rec ? orbit_process_big<NWo, CPLX, true, 256, kTeamCap, true>
+                                 : orbit_process_big<NWo, CPLX, true, 256, kTeamCap>);
+        auto block_k = ctx->orbit_block_threads == 512
+                           ? (rec ? orbit_process_big<NWo, CPLX, true, 512, kBlockCap, true>
+                                  : orbit_process_big<NWo, CPLX, true, 512, kBlockCap>)
+                           : (rec ? orbit_process_big<NWo, CPLX, true, 1024, kBlockCap, true>
+                                  : orbit_process_big<NWo, CPLX, true, 1024, kBlockCap>);
         // function attributes are set once per device (bit `device` of attr_devs)
         static u64 attr_devs = 0;
         static int team_per_sm = 1;
         if (!((attr_devs >> (ctx->device & 63)) & 1ull)) {
             for (auto k : {orbit_process_big<NWo, CPLX, true, 512, kBlockCap>,
-                           orbit_process_big<NWo, CPLX, true, 1024, kBlockCap>})
+                           orbit_process_big<NWo, CPLX, true, 1024, kBlockCap>,
+                           orbit_process_big<NWo, CPLX, true, 512, kBlockCap, true>,
+                           orbit_process_big<NWo, CPLX, true, 1024, kBlockCap, true>})
                 CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb));
             for (auto k : {orbit_process_big<NWo, CPLX, true, 128, kTeamCap>,
-                           orbit_process_big<NWo, CPLX, true, 256, kTeamCap>})
+                           orbit_process_big<NWo, CPLX, true, 256, kTeamCap>,
+                           orbit_process_big<NWo, CPLX, true, 128, kTeamCap, true>,
+                           orbit_process_big<NWo, CPLX, true, 256, kTeamCap, true>})
                 CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tt));
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                 &team_per_sm, orbit_process_big<NWo, CPLX, true, 256, kTeamCap>, 256, tt));
@@ -952,8 +963,12 @@ struct Engine {
             CK(cudaMemsetAsync(nretry, 0, 4, ctx->stream));
             {
                 PhaseScope ps(ctx, PH_ROT);
-                orbit_process_big<NWo, CPLX, false><<<grid, 1024, 0, ctx->stream>>>(in, out, sc, oc, a, bp, list,
-                                                                                   nleft, nullptr);
+                if (ctx->capture.n)
+                    orbit_process_big<NWo, CPLX, false, 1024, kBlockCap, true><<<grid, 1024, 0, ctx->stream>>>(
+                        in, out, sc, oc, a, bp, list, nleft, nullptr);
+                else
+                    orbit_process_big<NWo, CPLX, false><<<grid, 1024, 0, ctx->stream>>>(in, out, sc, oc, a, bp, list,
+                                                                                       nleft, nullptr);
                 OSTEP("orbit_process_big");
                 ctx->prof.kernel_launches++;
             }
@@ -1069,6 +1084,8 @@ struct Engine {
         if (!((attr_devs >> (ctx->device & 63)) & 1ull)) {
             CK(cudaFuncSetAttribute(orbit_process<NWo, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
+            CK(cudaFuncSetAttribute(orbit_process<NWo, CPLX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
             attr_devs |= 1ull << (ctx->device & 63);
         }
         const int G = ctx->num_sms * 8;
@@ -1116,7 +1133,11 @@ struct Engine {
                     const bool pdl = ctx->pdl;
                     const OrbitCounters* prev = j ? oc - 1 : nullptr;
                     CK(launch_k(pdl, orbit_gate, 1, 32, 0, ctx->stream, oc, prev, n_cur, sc.gmask + 1, nretry));
-                    CK(launch_k(pdl, orbit_classify<NWo, CPLX>, G, kBlock, 0, ctx->stream, in, out, sc, oc, a));
+                    if (a.active)
+                        CK(launch_k(pdl, orbit_classify<NWo, CPLX, true>, G, kBlock, 0, ctx->stream, in, out, sc, oc,
+                                    a));
+                    else
+                        CK(launch_k(pdl, orbit_classify<NWo, CPLX>, G, kBlock, 0, ctx->stream, in, out, sc, oc, a));
                     OSTEP("orbit_classify");
                     CK(launch_k(pdl, orbit_group<KW>, G, kBlock, 0, ctx->stream, sc, oc));
                     OSTEP("orbit_group");
@@ -1125,8 +1146,12 @@ struct Engine {
                     CK(launch_k(pdl, orbit_scatter<KW, CPLX>, G, kBlock, 0, ctx->stream, in, sc,
                                 (const OrbitCounters*)oc));
                     OSTEP("orbit_scatter");
-                    CK(launch_k(pdl, orbit_process<NWo, CPLX>, ctx->num_sms * 2, 32 * kOrbitWarps, smem, ctx->stream,
-                                in, out, sc, oc, a));
+                    if (a.cap.n)
+                        CK(launch_k(pdl, orbit_process<NWo, CPLX, true>, ctx->num_sms * 2, 32 * kOrbitWarps, smem,
+                                    ctx->stream, in, out, sc, oc, a));
+                    else
+                        CK(launch_k(pdl, orbit_process<NWo, CPLX>, ctx->num_sms * 2, 32 * kOrbitWarps, smem,
+                                    ctx->stream, in, out, sc, oc, a));
                     OSTEP("orbit_process");
                     ctx->prof.kernel_launches += 6;
                     rc = launch_big_tiers(in, out, sc, a, oc);

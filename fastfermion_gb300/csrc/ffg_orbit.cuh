@@ -308,7 +308,9 @@ __global__ void orbit_gate(OrbitCounters* cur, const OrbitCounters* prev, u64 n_
 }
 
 // A(Q) for every input term; group key; final terms go to the output.
-template <int NW, bool CPLX>
+// ACT: per-instance active rotations (a.active) are honoured; the plain
+// instantiation carries no trace of them.
+template <int NW, bool CPLX, bool ACT = false>
 __global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, StoreView out, OrbitScratch sc,
                                                          OrbitCounters* oc, OrbitBatchArgs a) {
     wait_prior_grid();
@@ -327,7 +329,7 @@ __global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, StoreView
         load_key<KW>(in, i, q);
         u64 A[kAW] = {};
         u64 U[KW] = {};
-        const u32 inst = a.active ? (u32)((q[a.inst_plane] >> a.inst_shift) & a.inst_mask) : 0u;
+        const u32 inst = ACT ? (u32)((q[a.inst_plane] >> a.inst_shift) & a.inst_mask) : 0u;
         if (a.qidx) {
             // candidates: the gates on the term's support
 #pragma unroll
@@ -340,7 +342,7 @@ __global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, StoreView
                     for (u32 e = __ldg(&a.qidx[qb]); e < e1; e++) {
                         const int t = (int)__ldg(&a.qidx[129 + e]);
                         if ((A[t >> 6] >> (t & 63)) & 1ull) continue;
-                        if (a.active && !gate_active(a, inst, t)) continue;
+                        if (ACT && !gate_active(a, inst, t)) continue;
                         u64 par = 0;
 #pragma unroll
                         for (int w = 0; w < NW; w++) par ^= (q[w] & gp[t][NW + w]) ^ (q[NW + w] & gp[t][w]);
@@ -354,7 +356,7 @@ __global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, StoreView
             }
         } else {
             for (int t = 0; t < a.k; t++) {
-                if (a.active && !gate_active(a, inst, t)) continue;
+                if (ACT && !gate_active(a, inst, t)) continue;
                 u64 par = 0;
 #pragma unroll
                 for (int w = 0; w < NW; w++) par ^= (q[w] & gp[t][NW + w]) ^ (q[NW + w] & gp[t][w]);
@@ -551,7 +553,9 @@ __device__ __forceinline__ void table_insert(OrbitTable<KW, CPLX>& T, const u64*
     }
 }
 
-template <int NW, bool CPLX>
+// REC: dropped partners are recorded into a.cap (capture runs); the plain
+// instantiation carries no trace of the record.
+template <int NW, bool CPLX, bool REC = false>
 __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, StoreView out, OrbitScratch sc,
                                                                   OrbitCounters* oc, OrbitBatchArgs a) {
     wait_prior_grid();
@@ -640,10 +644,10 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                         const cplx cj = {T.re[j], CPLX ? T.im[j] : 0.0};
                         cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
                         if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
-                        else if (a.cap.n && dQ <= a.cap.maxdeg)
+                        else if (REC && a.cap.n && dQ <= a.cap.maxdeg)
                             capture_drop<NW, CPLX>(a.cap, q, rot_partner<CPLX>(cj, gs, jK), G.gidx);
                         if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
-                        else if (a.cap.n && dK <= a.cap.maxdeg)
+                        else if (REC && a.cap.n && dK <= a.cap.maxdeg)
                             capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), G.gidx);
                         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
                         T.re[m] = ni.re;
@@ -672,7 +676,7 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                                 g_created++;
                                 g_xapps += a.k - 1 - t;
                             }
-                        } else if (a.cap.n && dK <= a.cap.maxdeg) {
+                        } else if (REC && a.cap.n && dK <= a.cap.maxdeg) {
                             capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), G.gidx);
                         }
                     }
@@ -805,7 +809,7 @@ constexpr size_t block_table_bytes() {
 // Block-level group processing with TB threads per block.  SM: the table lives
 // in dynamic shared memory (CAP members); otherwise in the block's
 // global-memory region of bp.
-template <int NW, bool CPLX, bool SM, int TB = 1024, u32 CAP = kBlockCap>
+template <int NW, bool CPLX, bool SM, int TB = 1024, u32 CAP = kBlockCap, bool REC = false>
 __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView out, OrbitScratch sc,
                                                           OrbitCounters* oc, OrbitBatchArgs a, BigPool bp,
                                                           const u32* list, u32 nlist, const u32* nlist_dev) {
@@ -913,10 +917,10 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                         const cplx cj = {tld<SM>(&G.re[j]), CPLX ? tld<SM>(&G.im[j]) : 0.0};
                         cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
                         if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
-                        else if (a.cap.n && dQ <= a.cap.maxdeg)
+                        else if (REC && a.cap.n && dQ <= a.cap.maxdeg)
                             capture_drop<NW, CPLX>(a.cap, q, rot_partner<CPLX>(cj, gs, jK), Gt.gidx);
                         if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
-                        else if (a.cap.n && dK <= a.cap.maxdeg)
+                        else if (REC && a.cap.n && dK <= a.cap.maxdeg)
                             capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
                         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
                         G.re[m] = ni.re;
@@ -945,7 +949,7 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                                 g_created++;
                                 g_xapps += a.k - 1 - t;
                             }
-                        } else if (a.cap.n && dK <= a.cap.maxdeg) {
+                        } else if (REC && a.cap.n && dK <= a.cap.maxdeg) {
                             capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
                         }
                     }
