@@ -214,6 +214,7 @@ struct ffg_ctx {
     RawBuf bigpool;                 // global-memory tables of large orbit groups
     const BatchCtx* batch = nullptr;  // set while a batched propagation runs
     CaptureArgs capture{};            // set while a capture propagation runs (n null: off)
+    const CaptureArgs* capture_dev = nullptr;  // its device copy (the kernels' argument)
     RawBuf capbuf;                    // capture records and their index
     ffg_profile prof{};
     std::vector<PendingEvent> events;
@@ -882,7 +883,7 @@ struct Engine {
         const size_t tb = block_table_bytes<KW, CPLX>();
         const size_t tt = block_table_bytes<KW, CPLX, kTeamCap>();
         // the tier kernels at each thread count (options orbit_team_threads, orbit_block_threads)
-        const bool rec = ctx->capture.n != nullptr;  // capture runs record the dropped partners
+        const bool rec = ctx->capture_dev != nullptr;  // capture runs record the dropped partners
         auto team_k = ctx->orbit_team_threads == 128
                           ? (rec ? orbit_process_big<NWo, CPLX, true, 128, kTeamCap, true>
                                  : orbit_process_big<NWo, CPLX, true, 128, kTeamCap>)
@@ -963,7 +964,7 @@ struct Engine {
             CK(cudaMemsetAsync(nretry, 0, 4, ctx->stream));
             {
                 PhaseScope ps(ctx, PH_ROT);
-                if (ctx->capture.n)
+                if (ctx->capture_dev)
                     orbit_process_big<NWo, CPLX, false, 1024, kBlockCap, true><<<grid, 1024, 0, ctx->stream>>>(
                         in, out, sc, oc, a, bp, list, nleft, nullptr);
                 else
@@ -1064,7 +1065,7 @@ struct Engine {
                 a.act_r0 = (int)ctx->batch->nrot - 1 - j.g0;
             }
         }
-        a.cap = ctx->capture;
+        a.cap = ctx->capture_dev;
         return a;
     }
 
@@ -1146,7 +1147,7 @@ struct Engine {
                     CK(launch_k(pdl, orbit_scatter<KW, CPLX>, G, kBlock, 0, ctx->stream, in, sc,
                                 (const OrbitCounters*)oc));
                     OSTEP("orbit_scatter");
-                    if (a.cap.n)
+                    if (a.cap)
                         CK(launch_k(pdl, orbit_process<NWo, CPLX, true>, ctx->num_sms * 2, 32 * kOrbitWarps, smem,
                                     ctx->stream, in, out, sc, oc, a));
                     else
@@ -2580,7 +2581,7 @@ int ffg_pauli_propagate_capture(ffg_ctx* ctx, const uint64_t* keys, const double
         u64 cap = 1ull << 16;
         for (int attempt = 0; attempt < 8; attempt++) {
             const size_t need = align256(4 * cap * 8) + 2 * align256(cap * 8) + align256(cap * 4) +
-                                align256(2 * cap * 4) + 256;
+                                align256(2 * cap * 4) + 256 + align256(sizeof(CaptureArgs));
             int rc = ensure_buf(ctx, ctx->capbuf, need);
             if (rc) return rc;
             char* p = ctx->capbuf.p;
@@ -2600,10 +2601,14 @@ int ffg_pauli_propagate_capture(ffg_ctx* ctx, const uint64_t* keys, const double
             cp.maxdeg = capdeg;
             cp.min_abs = min_abs;
             CK(cudaMemsetAsync(cp.slot, 0, 2 * cap * 4 + 256, ctx->stream));  // index and counter
+            CaptureArgs* cdev = (CaptureArgs*)(p + 256);
+            CK(cudaMemcpyAsync(cdev, &cp, sizeof cp, cudaMemcpyHostToDevice, ctx->stream));
             ctx->capture = cp;
+            ctx->capture_dev = cdev;
             ffg_result* r = nullptr;
             rc = pauli_propagate_impl(ctx, keys, re, im, n, gates, ngates, params, on_device, &r, true);
             ctx->capture = CaptureArgs{};
+            ctx->capture_dev = nullptr;
             if (rc) return rc;
             u64 claimed = 0;
             CK(cudaMemcpyAsync(&claimed, cp.n, 8, cudaMemcpyDeviceToHost, ctx->stream));

@@ -155,7 +155,7 @@ struct OrbitBatchArgs {
     const u64* active;
     u32 active_words;
     int act_r0;
-    CaptureArgs cap;
+    const CaptureArgs* cap;  // record of dropped partners (device copy; null: off)
 };
 
 // whether batch gate t acts on instance inst
@@ -553,10 +553,10 @@ __device__ __forceinline__ void table_insert(OrbitTable<KW, CPLX>& T, const u64*
     }
 }
 
-// REC: dropped partners are recorded into a.cap (capture runs); the plain
+// REC: dropped partners are recorded into *a.cap (capture runs); the plain
 // instantiation carries no trace of the record.
 template <int NW, bool CPLX, bool REC = false>
-__global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, StoreView out, OrbitScratch sc,
+__global__ void __launch_bounds__(32 * kOrbitWarps, 4) orbit_process(StoreView in, StoreView out, OrbitScratch sc,
                                                                   OrbitCounters* oc, OrbitBatchArgs a) {
     wait_prior_grid();
     constexpr int KW = 2 * NW;
@@ -644,11 +644,11 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                         const cplx cj = {T.re[j], CPLX ? T.im[j] : 0.0};
                         cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
                         if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
-                        else if (REC && a.cap.n && dQ <= a.cap.maxdeg)
-                            capture_drop<NW, CPLX>(a.cap, q, rot_partner<CPLX>(cj, gs, jK), G.gidx);
+                        else if (REC && a.cap && dQ <= a.cap->maxdeg)
+                            capture_drop<NW, CPLX>(*a.cap, q, rot_partner<CPLX>(cj, gs, jK), G.gidx);
                         if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
-                        else if (REC && a.cap.n && dK <= a.cap.maxdeg)
-                            capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), G.gidx);
+                        else if (REC && a.cap && dK <= a.cap->maxdeg)
+                            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), G.gidx);
                         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
                         T.re[m] = ni.re;
                         T.re[j] = nj.re;
@@ -676,8 +676,8 @@ __global__ void __launch_bounds__(32 * kOrbitWarps) orbit_process(StoreView in, 
                                 g_created++;
                                 g_xapps += a.k - 1 - t;
                             }
-                        } else if (REC && a.cap.n && dK <= a.cap.maxdeg) {
-                            capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), G.gidx);
+                        } else if (REC && a.cap && dK <= a.cap->maxdeg) {
+                            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), G.gidx);
                         }
                     }
                 }
@@ -917,11 +917,11 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                         const cplx cj = {tld<SM>(&G.re[j]), CPLX ? tld<SM>(&G.im[j]) : 0.0};
                         cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
                         if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
-                        else if (REC && a.cap.n && dQ <= a.cap.maxdeg)
-                            capture_drop<NW, CPLX>(a.cap, q, rot_partner<CPLX>(cj, gs, jK), Gt.gidx);
+                        else if (REC && a.cap && dQ <= a.cap->maxdeg)
+                            capture_drop<NW, CPLX>(*a.cap, q, rot_partner<CPLX>(cj, gs, jK), Gt.gidx);
                         if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
-                        else if (REC && a.cap.n && dK <= a.cap.maxdeg)
-                            capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
+                        else if (REC && a.cap && dK <= a.cap->maxdeg)
+                            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
                         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
                         G.re[m] = ni.re;
                         G.re[j] = nj.re;
@@ -949,8 +949,8 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                                 g_created++;
                                 g_xapps += a.k - 1 - t;
                             }
-                        } else if (REC && a.cap.n && dK <= a.cap.maxdeg) {
-                            capture_drop<NW, CPLX>(a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
+                        } else if (REC && a.cap && dK <= a.cap->maxdeg) {
+                            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
                         }
                     }
                 }
