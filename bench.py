@@ -303,6 +303,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-roofline", action="store_true")
+    ap.add_argument("--sweep", default="separate", choices=["separate", "batched"],
+                    help="Pauli workloads: one propagation per theta_h (separate), or all theta_h as "
+                         "instances of one batched propagation with per-instance angles (batched)")
     ap.add_argument("--thetas", default=None,
                     help="comma-separated subset of theta_h (profiling runs; not a bench line)")
     a = ap.parse_args()
@@ -692,9 +695,24 @@ def main():
     l2 = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 512 MB > L2
     torch.cuda.synchronize()
 
+    batched_sweep = args.sweep == "batched" and wl.kind == "pauli" and len(tabs) > 1
+    if batched_sweep:
+        # every theta_h as an instance with its own angles: the same terms,
+        # bit for bit, as the separate propagations (ffg_pauli_propagate_batched)
+        bk = np.repeat(hk, len(tabs), axis=1)
+        bre = np.repeat(hre, len(tabs))
+        boff = np.arange(len(tabs) + 1, dtype=np.int64) * hre.size
+        bth = np.stack([t["theta"][t["kind"] == 0] for t in tabs])
+        bparams = dict(wl.params)
+
     def step_device(profiling=False):
         ctx.set_profiling(profiling)
         apps, emits, launches, rot_s, nrot = 0, 0, 0, 0.0, 0
+        if batched_sweep:
+            _, h = ctx.pauli_propagate_batched(bk, bre, boff, tabs[0], bth, bparams, 0)
+            pr = ctx.profile()
+            h.free()
+            return pr["apps"], pr["emits"], pr["kernel_launches"], pr["seconds_rotations"], pr["n_gates"]
         for tab in tabs:
             r = wl.propagate(ctx, dk.data_ptr(), dre.data_ptr(), dim.data_ptr(), tab, n=hre.size)
             pr = ctx.profile()
@@ -751,6 +769,14 @@ def main():
     e2e_times, h2d, d2h = [], 0, 0
     for _ in range(0 if args.no_e2e else max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
+        if batched_sweep:
+            expect, h = ctx.pauli_propagate_batched(bk, bre, boff, tabs[0], bth, bparams, 0)
+            keys, re, inst = h.copy()
+            h.free()
+            d2h += keys.nbytes + re.nbytes + inst.nbytes + expect.nbytes
+            h2d += bk.nbytes + bre.nbytes + boff.nbytes + bth.nbytes + tabs[0].nbytes
+            e2e_times.append(time.perf_counter() - t0)
+            continue
         for tab in tabs:
             r = wl.propagate(ctx, hk, hre, him, tab)
             keys, re, im = r.copy()
@@ -772,7 +798,7 @@ def main():
             "metric": wl.metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(wl.config(), apps_per_step=apps_tot / args.steps,
+            "config": dict(wl.config(), apps_per_step=apps_tot / args.steps, sweep=args.sweep,
                            l2="flushed between steps (512 MB write)", parallelism=f"replicas{ws}"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None,

@@ -2068,12 +2068,34 @@ int batch_forward(ffg_batch* h, const uint64_t* keys, const double* re, size_t n
     std::string err;
     if (E.build_records(h->ops, h->truncs, h->binfo, gate_of_op, h->recs, err)) return set_err(ctx, FFG_ERR_ARG, err);
     ctx->batch = &h->bc;
-    for (size_t r = 0; r < h->recs.size() && !rc; r++) {
-        if (h->every > 0 && r % (size_t)h->every == 0) rc = E.snapshot(h->recs[r]);
-        if (!rc) {
-            h->recs[r].n_in = ctx->h_ctr->n;
-            rc = E.exec_record(h->recs[r], h->maxdeg);
+    if (h->every > 0) {
+        for (size_t r = 0; r < h->recs.size() && !rc; r++) {
+            if (r % (size_t)h->every == 0) rc = E.snapshot(h->recs[r]);
+            if (!rc) {
+                h->recs[r].n_in = ctx->h_ctr->n;
+                rc = E.exec_record(h->recs[r], h->maxdeg);
+            }
         }
+    } else {
+        // no adjoint: consecutive orbit batches run in windows (one host round
+        // trip per window), Clifford ranges through the persistent kernel
+        std::vector<typename Engine<KW, false, true>::OrbitJob> jobs;
+        auto flush = [&]() {
+            int r2 = FFG_OK;
+            if (!jobs.empty()) r2 = E.exec_orbit_window(jobs.data(), (int)jobs.size(), h->maxdeg);
+            jobs.clear();
+            return r2;
+        };
+        for (size_t r = 0; r < h->recs.size() && !rc; r++) {
+            const AdjRecord& rec = h->recs[r];
+            if (rec.type == AdjRecord::ORBIT) {
+                jobs.push_back({rec.g0, rec.k, rec.has_trunc ? &rec.trunc : nullptr});
+            } else {
+                rc = flush();
+                if (!rc) rc = E.exec_record(rec, h->maxdeg);
+            }
+        }
+        if (!rc) rc = flush();
     }
     if (!rc) rc = E.finish();
     ctx->batch = nullptr;

@@ -242,3 +242,29 @@ def test_torch_autograd_function():
     # per-instance sums run in no fixed order: equal up to rounding
     np.testing.assert_allclose(e.detach().numpy(), r.expect, rtol=0, atol=1e-14)
     np.testing.assert_allclose(t.grad.numpy(), r.gradient(w.numpy()), rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.gpu
+def test_theta_sweep_as_instances_matches_reference_fixtures():
+    """The headline theta_h sweep as instances of one batched propagation
+    (per-instance angles, no checkpoints: orbit windows): every instance's
+    term set equals the reference's own result for that theta_h."""
+    from golden_io import assert_same_terms, load
+    from fastfermion_gb300 import _native
+    names = ["cfg2_kicked_ising_0p1000", "cfg2_kicked_ising_0p5000", "cfg2_kicked_ising_0p9000"]
+    fxs = [load(n) for n in names]
+    tabs = [fx["gates"] for fx in fxs]
+    k = np.concatenate([fx["obs_keys"] for fx in fxs], axis=1)
+    re = np.concatenate([fx["obs_re"] for fx in fxs])
+    off = np.array([0, 1, 2, 3], dtype=np.int64)
+    th = np.stack([t["theta"][t["kind"] == 0] for t in tabs])
+    p = dict(maxdegree=int(fxs[0]["maxdegree"]), topk=0, mincoeff=float(fxs[0]["mincoeff"]), max_xweight=-1,
+             xtrunc_period=1, batched=1, deterministic=0)
+    ctx = _native.context(0)
+    expect, h = ctx.pauli_propagate_batched(k, re, off, tabs[0], th, p, 0)
+    keys, cre, inst = h.copy()
+    for i, fx in enumerate(fxs):
+        sel = inst == i
+        assert_same_terms((keys[:, sel], cre[sel], np.zeros(int(sel.sum()))),
+                          (fx["res_keys"], fx["res_re"], fx["res_im"]))
+        assert abs(expect[i] - float(fx["overlap"][0])) <= 1e-12
