@@ -258,6 +258,33 @@ __device__ __forceinline__ bool survives(const u64* key, cplx c, const OrbitBatc
     return true;
 }
 
+// Appends the entries of the calling lanes that keep theirs with one atomic
+// per set of converged lanes (warp ballot, then each lane's rank in it).
+// Every converged lane calls it, keep or not.
+template <int KW, bool CPLX>
+__device__ __forceinline__ void out_append_warp(const StoreView& o, OrbitCounters* oc, const u64* key, cplx c,
+                                                bool keep) {
+    const unsigned mask = __activemask();
+    const unsigned ball = __ballot_sync(mask, keep);
+    if (!ball) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ball) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&oc->n_out, (u64)__popc(ball));
+    base = __shfl_sync(mask, base, leader);
+    if (!keep) return;
+    const u64 pos = base + (u64)__popc(ball & ((1u << lane) - 1u));
+    if (pos >= o.cap) {
+        atomicOr(&oc->overflow, 1u);
+        return;
+    }
+#pragma unroll
+    for (int w = 0; w < KW; w++) o.key[(u64)w * o.cap + pos] = key[w];
+    o.re[pos] = c.re;
+    if (CPLX) o.im[pos] = c.im;
+    o.dead[pos] = 0;
+}
+
 template <int KW, bool CPLX>
 __device__ __forceinline__ void out_append(const StoreView& o, OrbitCounters* oc, const u64* key, cplx c) {
     const u64 pos = atomicAdd(&oc->n_out, 1ull);
@@ -373,7 +400,7 @@ __global__ void __launch_bounds__(kBlock) orbit_classify(StoreView in, StoreView
         if (!any) {
             sc.rep[i] = 0xffffffffu;
             const cplx c = load_coef<CPLX>(in, i);
-            if (survives<NW, CPLX>(q, c, a)) out_append<KW, CPLX>(out, oc, q, c);
+            out_append_warp<KW, CPLX>(out, oc, q, c, survives<NW, CPLX>(q, c, a));
             continue;
         }
 #pragma unroll
@@ -708,7 +735,7 @@ __global__ void __launch_bounds__(32 * kOrbitWarps, 4) orbit_process(StoreView i
         }
         for (int m = lane; m < cnt; m += 32) {
             const cplx c = {T.re[m], CPLX ? T.im[m] : 0.0};
-            if (survives<NW, CPLX>(T.key[m], c, a)) out_append<KW, CPLX>(out, oc, T.key[m], c);
+            out_append_warp<KW, CPLX>(out, oc, T.key[m], c, survives<NW, CPLX>(T.key[m], c, a));
         }
         __syncwarp();
     }
@@ -981,7 +1008,7 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
 #pragma unroll
             for (int w = 0; w < KW; w++) k[w] = tld<SM>(&G.key[(u64)w * rcap + m]);
             const cplx c = {tld<SM>(&G.re[m]), CPLX ? tld<SM>(&G.im[m]) : 0.0};
-            if (survives<NW, CPLX>(k, c, a)) out_append<KW, CPLX>(out, oc, k, c);
+            out_append_warp<KW, CPLX>(out, oc, k, c, survives<NW, CPLX>(k, c, a));
         }
         __syncthreads();
     }
