@@ -178,7 +178,7 @@ class Context:
     OPTIONS = ("orbit_route_big", "orbit_team", "orbit_window", "orbit_min_gates", "orbit_qidx", "pdl",
                "morbit", "morbit_min_gates", "morbit_route_big", "merge_sort", "orbit_team_threads",
                "orbit_block_threads", "min_capacity", "store_headroom", "group_region_cap",
-               "barrier_limit_kcycles")
+               "barrier_limit_kcycles", "orbit", "persistent", "persist_blocks_per_sm", "group_d", "orbit_stats")
 
     def set_option(self, name, value):
         self.check(self.L.ffg_set_option(self.h, name.encode(), int(value)))

@@ -163,9 +163,9 @@ struct ffg_ctx {
     size_t ties_cap = 0;
     std::string err;
     bool profiling = false;
-    int group_d = 1;  // rotations fused per pass (1..4), FFG_GROUP_D overrides
-    bool persistent = true;  // one cooperative launch per run of ops (FFG_PERSISTENT=0 disables)
-    int persist_blocks_per_sm = 2;  // FFG_PERSIST_BPS overrides
+    int group_d = 1;  // rotations fused per pass (1..4; option group_d)
+    bool persistent = true;  // one cooperative launch per run of ops (option persistent)
+    int persist_blocks_per_sm = 2;  // blocks per SM of the persistent kernel (option persist_blocks_per_sm)
     PersistState* d_ps = nullptr;
     DevOp* d_ops = nullptr;
     size_t ops_cap = 0;
@@ -177,13 +177,13 @@ struct ffg_ctx {
     size_t truncs_cap = 0;
     GroupArgs<2>* d_groups2 = nullptr;
     size_t groups2_cap = 0;
-    bool orbit = true;          // batch-orbit path for long commuting runs (FFG_ORBIT=0 disables)
+    bool orbit = true;          // batch-orbit path for long commuting runs (option orbit)
     int orbit_min_gates = 4;    // shortest run sent to the batch-orbit path
-    int orbit_route_big = 8;    // |A| from which a group skips the warp-level pass (FFG_ORBIT_ROUTE)
-    bool orbit_team = true;     // 256-thread team pass before the 1024-thread pass (FFG_ORBIT_TEAM=0 disables)
-    bool morbit = true;         // batch-orbit path for commuting Majorana runs (FFG_MORBIT=0 disables)
-    bool pdl = true;            // programmatic dependent launch of the orbit kernels (FFG_PDL=0 disables)
-    bool orbit_qidx = true;     // classify against the gates on each term's support (FFG_ORBIT_QIDX=0 disables)
+    int orbit_route_big = 8;    // |A| from which a group skips the warp-level pass (option orbit_route_big)
+    bool orbit_team = true;     // 256-thread team pass before the 1024-thread pass (option orbit_team)
+    bool morbit = true;         // batch-orbit path for commuting Majorana runs (option morbit)
+    bool pdl = true;            // programmatic dependent launch of the orbit kernels (option pdl)
+    bool orbit_qidx = true;     // classify against the gates on each term's support (option orbit_qidx)
     int orbit_window = kOrbitWindowMax;  // orbit batches per host round trip (1..kOrbitWindowMax)
     bool merge_sort = false;    // per-gate sort-and-reduce merge instead of the hash / orbit paths
     int orbit_team_threads = 256;   // threads of a team-tier group (128 or 256)
@@ -193,11 +193,12 @@ struct ffg_ctx {
     int morbit_min_gates = 2;   // shortest Majorana run sent to the batch-orbit path
     u64 min_capacity = 1ull << 16;      // smallest term-store capacity (option min_capacity)
     long long barrier_limit = kBarrierLimitCycles;  // grid-barrier wait limit, cycles (option barrier_limit_kcycles)
+    bool orbit_stats = false;           // print per-batch group statistics to stderr (option orbit_stats)
     int store_headroom = 4;             // orbit windows size their stores for this many times
                                         // the entering terms (option store_headroom)
     u64 group_region_cap = 1ull << 14;  // members of a first global-memory group region (Pauli;
                                         // Majorana starts at a quarter of it)
-    int morbit_route_big = 12;  // |A| from which a Majorana group skips the warp tier (FFG_MORBIT_ROUTE);
+    int morbit_route_big = 12;  // |A| from which a Majorana group skips the warp tier (option morbit_route_big);
                                 // 6x6 Hubbard: 323 ms at 12 or 16, 329 ms at 10, 356 ms at 8
     MBatchGate* d_mgates = nullptr;
     size_t mgates_cap = 0;
@@ -1200,7 +1201,7 @@ struct Engine {
                 ctx->prof.orbit_max_group = std::max<int64_t>(ctx->prof.orbit_max_group, oc.max_members);
                 ctx->prof.orbit_batches++;
                 ctx->prof.orbit_groups += oc.ngroups;
-                if (getenv("FFG_ORBIT_STATS")) {
+                if (ctx->orbit_stats) {
                     fprintf(stderr, "batch k=%d n_in=%llu groups=%u big=%u wasted=%u out=%llu |", jb.k,
                             (unsigned long long)oc.n_in, oc.ngroups, oc.nbig, oc.wasted,
                             (unsigned long long)oc.n_out);
@@ -2367,23 +2368,6 @@ int ffg_create(ffg_ctx** out, int device) {
     *out = nullptr;
     ffg_ctx* ctx = new ffg_ctx();
     ctx->device = device;
-    if (const char* d = getenv("FFG_GROUP_D")) {
-        const int v = atoi(d);
-        if (v >= 1 && v <= kGroupD) ctx->group_d = v;
-    }
-    if (const char* d = getenv("FFG_PERSISTENT")) ctx->persistent = atoi(d) != 0;
-    if (const char* d = getenv("FFG_PERSIST_BPS")) ctx->persist_blocks_per_sm = std::max(1, atoi(d));
-    if (const char* d = getenv("FFG_ORBIT")) ctx->orbit = atoi(d) != 0;
-    if (const char* d = getenv("FFG_ORBIT_MIN")) ctx->orbit_min_gates = std::max(1, atoi(d));
-    if (const char* d = getenv("FFG_ORBIT_ROUTE")) ctx->orbit_route_big = std::max(1, atoi(d));
-    if (const char* d = getenv("FFG_ORBIT_TEAM")) ctx->orbit_team = atoi(d) != 0;
-    if (const char* d = getenv("FFG_MORBIT")) ctx->morbit = atoi(d) != 0;
-    if (const char* d = getenv("FFG_PDL")) ctx->pdl = atoi(d) != 0;
-    if (const char* d = getenv("FFG_ORBIT_QIDX")) ctx->orbit_qidx = atoi(d) != 0;
-    if (const char* d = getenv("FFG_TEAM_THREADS")) ctx->orbit_team_threads = atoi(d) == 128 ? 128 : 256;
-    if (const char* d = getenv("FFG_BLOCK_THREADS")) ctx->orbit_block_threads = atoi(d) == 512 ? 512 : 1024;
-    if (const char* d = getenv("FFG_MORBIT_MIN")) ctx->morbit_min_gates = std::max(1, atoi(d));
-    if (const char* d = getenv("FFG_MORBIT_ROUTE")) ctx->morbit_route_big = std::max(1, atoi(d));
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -3539,6 +3523,15 @@ const OptionRef kOptions[] = {
          c->barrier_limit = v * 1000;
          return true;
      }},
+    {"persistent", [](const ffg_ctx* c) { return (int)c->persistent; },
+     [](ffg_ctx* c, int64_t v) { c->persistent = v != 0; return true; }},
+    {"orbit", [](const ffg_ctx* c) { return (int)c->orbit; }, [](ffg_ctx* c, int64_t v) { c->orbit = v != 0; return true; }},
+    {"group_d", [](const ffg_ctx* c) { return c->group_d; },
+     [](ffg_ctx* c, int64_t v) { if (v < 1 || v > kGroupD) return false; c->group_d = (int)v; return true; }},
+    {"persist_blocks_per_sm", [](const ffg_ctx* c) { return c->persist_blocks_per_sm; },
+     [](ffg_ctx* c, int64_t v) { if (v < 1 || v > 8) return false; c->persist_blocks_per_sm = (int)v; return true; }},
+    {"orbit_stats", [](const ffg_ctx* c) { return (int)c->orbit_stats; },
+     [](ffg_ctx* c, int64_t v) { c->orbit_stats = v != 0; return true; }},
     {"store_headroom", [](const ffg_ctx* c) { return c->store_headroom; },
      [](ffg_ctx* c, int64_t v) {
          if (v < 1 || v > 64) return false;

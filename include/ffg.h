@@ -146,6 +146,12 @@ void* ffg_stream(const ffg_ctx* ctx);
  *   morbit_route_big  |A| from which a Majorana group skips the warp tier (12)
  *   merge_sort        1: Pauli rotations one at a time with a radix sort and a
  *                     segmented reduce instead of the hash index / orbit paths (0)
+ *   orbit             1: batch-orbit path for commuting Pauli runs (1)
+ *   persistent        1: one cooperative launch per run of per-gate ops; 0: one
+ *                     launch per op (1)
+ *   persist_blocks_per_sm  blocks per SM of the persistent kernel, 1..8 (2)
+ *   group_d           rotations fused per pass of the per-gate paths, 1..4 (1)
+ *   orbit_stats       1: per-batch group statistics on stderr (0)
  *   min_capacity      smallest term-store capacity, a power of two >= 64 (65536)
  *   store_headroom    orbit windows size their output stores for this many times
  *                     the entering terms, 1..64 (4); a batch that outgrows its

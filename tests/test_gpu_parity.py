@@ -205,3 +205,33 @@ def test_large_results_have_distinct_keys():
         tau = float(fx["mincoeff"])
         if tau > 0:
             assert np.all(np.hypot(re, im) > tau), name
+
+
+ENGINE_PATHS = [("persistent", 0), ("orbit", 0), ("group_d", 2), ("group_d", 4), ("morbit", 0),
+                ("persist_blocks_per_sm", 1)]
+PATH_FIXTURES = ["ref_tfim", "ref_tfim_unbatched", "ref_mixed_clifford", "cfg1_chain", "rand_pauli_00",
+                 "rand_pauli_05", "ref_heisenberg", "ref_majorana_1", "rand_majorana_03"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("option,value", ENGINE_PATHS, ids=[f"{o}={v}" for o, v in ENGINE_PATHS])
+def test_engine_paths_match_reference(option, value):
+    """Every alternative engine path (one launch per op, no orbit path, fused
+    rotation groups, the Majorana per-gate kernel, one persistent block per SM)
+    gives the reference's term sets."""
+    from fastfermion_gb300 import _native
+    ctx = _native.context(0)
+    old = ctx.get_option(option)
+    try:
+        ctx.set_option(option, value)
+        for name in PATH_FIXTURES:
+            fx = load(name)
+            if int(fx["topk"]) > 0:
+                continue
+            keys, re, im = run_gpu(fx).copy()
+            if "res_keys" in fx:
+                assert_same_terms((keys, re, im), (fx["res_keys"], fx["res_re"], fx["res_im"])), name
+            else:
+                assert checksum(keys, re, im) == str(fx["checksum"]), name
+    finally:
+        ctx.set_option(option, old)
