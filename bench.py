@@ -4,8 +4,11 @@ the 100-qubit 10x10 kicked-Ising circuit (20 Trotter steps; RZZ(-pi/2) on the
 maximum weight 8, coefficient threshold 1e-6), swept over
 theta_h in {0.1, 0.3, 0.5, 0.7, 0.9, 1.1, pi/2}.
 
-One step = the whole theta_h sweep (7 propagations).  Term-gate applications
-("apps") = sum over rotation gates of the live terms entering the gate.
+One step = the whole theta_h sweep: by default its 7 values run as instances
+of one batched propagation with per-instance angles (each instance's terms
+bit-identical to its own propagation); --sweep separate runs 7 propagations.
+Term-gate applications ("apps") = sum over rotation gates of the live terms
+entering the gate.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--workload kicked_ising|kicked_ising_w10|hubbard|hea]
@@ -303,7 +306,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-roofline", action="store_true")
-    ap.add_argument("--sweep", default="separate", choices=["separate", "batched"],
+    ap.add_argument("--sweep", default="batched", choices=["separate", "batched"],
                     help="Pauli workloads: one propagation per theta_h (separate), or all theta_h as "
                          "instances of one batched propagation with per-instance angles (batched)")
     ap.add_argument("--thetas", default=None,
@@ -416,8 +419,22 @@ class ClockSampler:
 # CPU baseline (the oracle's port of the reference algorithm)
 # ---------------------------------------------------------------------------
 def cpu_baseline(wl, tabs):
-    apps, dt, cores, desc = wl.cpu_sample(tabs, os.cpu_count() or 1, min_seconds=10.0)
-    out = {"value": apps / dt, "unit": UNIT, "cores": cores, "kind": "port",
+    """The reference itself (built from its own sources in baseline/_ref) where
+    the workload has a reference sample and the build exists, else the oracle's
+    port; about 10 s of host time."""
+    cores = os.cpu_count() or 1
+    ref = reference_module() if hasattr(wl, "ref_sample") else None
+    if ref is not None:
+        cache, apps, dt = {}, 0, 0.0
+        while dt < 10.0:
+            a, t, cores, desc = wl.ref_sample(ref, cores, cache)
+            apps += a
+            dt += t
+        kind = "reference"
+    else:
+        apps, dt, cores, desc = wl.cpu_sample(tabs, cores, min_seconds=10.0)
+        kind = "port"
+    out = {"value": apps / dt, "unit": UNIT, "cores": cores, "kind": kind,
            "sample": f"{desc} ({apps} apps, {dt:.1f} s)"}
     if hasattr(wl, "serial_sample"):
         apps, dt, desc = wl.serial_sample()
@@ -750,6 +767,24 @@ def main():
     apps_all = allsum(dist, apps_tot)
     value = apps_all / t_max
 
+    # the same sweep as one propagation per theta_h, for comparison (not the value)
+    separate = None
+    if batched_sweep and not args.no_e2e:
+        batched_sweep = False
+        ts = []
+        for _ in range(2):
+            l2.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            a_sep = step_device()[0]
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        separate = a_sep / min(ts)
+        batched_sweep = True
+
     # roofline: the per-gate algorithm's bytes (B_g = (S + 8)(2 N_g + E_g) summed
     # over the rotations of a step) over the same unprofiled CUDA-event step time
     # as `value`.  The orbit engine does not move those bytes (groups live in
@@ -799,6 +834,11 @@ def main():
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": dict(wl.config(), apps_per_step=apps_tot / args.steps, sweep=args.sweep,
+                           sweep_note=("all theta_h as instances of one batched propagation "
+                                       "(ffg_pauli_propagate_batched, per-instance angles; each instance's terms "
+                                       "bit-identical to its own propagation)") if batched_sweep else
+                           "one propagation per theta_h (ffg_pauli_propagate)",
+                           separate_propagations_apps_per_s=separate,
                            l2="flushed between steps (512 MB write)", parallelism=f"replicas{ws}"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None,
