@@ -195,19 +195,17 @@ __global__ void __launch_bounds__(kThreads, 1)
 // ---------------------------------------------------------------------------
 // inference
 // ---------------------------------------------------------------------------
-struct __align__(1024) FwdSmem {
-    uint8_t w[kFwdImgBytes];        // W1 | W2 | W3 images, bias block
-    uint8_t x[kTile * kIn * 2];     // input tile image (K = 32)
-    uint8_t h[kTile * kHid * 2];    // hidden activations image (K = 128)
-    uint64_t bar_w, bar_mma;
-    uint32_t tmem;
-};
+// Inference runs 8 warps per CTA: warps w and w + 4 read the same TMEM lane
+// quarter (rows 32 (w % 4) ..) and split the 128 columns of every layer between
+// them, so the FP32 epilogue (bias, GELU, BF16 packing), which bounds this
+// kernel, has twice the warps and half the serial work per thread.
+constexpr int kFwdThreads = 256;
 
-// hidden-layer epilogue: bias + GELU of the accumulator row into the next
-// layer's operand image
-__device__ __forceinline__ void hidden_epilogue(uint32_t trow, const float* bias, uint8_t* img, int r) {
+// hidden-layer epilogue of one thread: bias + GELU of columns c0 .. c0+63 of
+// the accumulator row into the next layer's operand image
+__device__ __forceinline__ void hidden_epilogue64(uint32_t trow, const float* bias, uint8_t* img, int r, int c0) {
 #pragma unroll 1
-    for (int c = 0; c < kHid; c += 16) {
+    for (int c = c0; c < c0 + kHid / 2; c += 16) {
         float v[16];
         tmem_ld16(trow + (uint32_t)c, v);
 #pragma unroll
@@ -216,12 +214,24 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t trow, const float* bias
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+struct __align__(1024) FwdSmem {
+    uint8_t w[kFwdImgBytes];        // W1 | W2 | W3 images, bias block
+    uint8_t x[kTile * kIn * 2];     // input tile image (K = 32)
+    uint8_t h[kTile * kHid * 2];    // hidden activations image (K = 128)
+    float part[kTile];              // the second column half's share of each row's output
+    uint64_t bar_w, bar_mma;
+    uint32_t tmem;
+};
+
+__global__ void __launch_bounds__(kFwdThreads, 1)
     mlp_forward_kernel(const uint8_t* __restrict__ wimg, const __nv_bfloat16* __restrict__ x, size_t n,
                        float* __restrict__ y, int* status) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     FwdSmem& S = *reinterpret_cast<FwdSmem*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int r = 32 * (warp & 3) + (tid & 31);  // row of the tile = TMEM lane
+    const int half = warp >> 2;                  // column half of this thread
+    const int c0 = half * (kHid / 2);
     const size_t ntiles = (n + kTile - 1) / kTile;
     if (tid == 0) {
         mbar_init(&S.bar_w, 1);
@@ -233,7 +243,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = S.tmem;
-    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+    const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
     if (tid == 0) {
         mbar_expect_tx(&S.bar_w, kFwdImgBytes);
         bulk_g2s(S.w, wimg, kFwdImgBytes, &S.bar_w);
@@ -243,8 +253,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t sx = smem_u32(S.x), sh = smem_u32(S.h);
     uint32_t phase = 0;
     for (size_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-        const size_t row = tile * kTile + tid;
-        stage_x(S.x, tid, x, n, row);
+        const size_t row = tile * kTile + r;
+        {  // each half stages two of the row's four 16-byte input chunks
+            uint4 v[2] = {};
+            if (row < n) {
+                const uint4* src = reinterpret_cast<const uint4*>(x + row * kIn) + 2 * half;
+                v[0] = __ldg(src);
+                v[1] = __ldg(src + 1);
+            }
+            *reinterpret_cast<uint4*>(S.x + img_off(r, 16 * half, kIn)) = v[0];
+            *reinterpret_cast<uint4*>(S.x + img_off(r, 16 * half + 8, kIn)) = v[1];
+        }
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -258,7 +277,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         phase ^= 1;
         if (!ok) break;
         tc_fence_after();
-        hidden_epilogue(trow, bias, S.h, tid);
+        hidden_epilogue64(trow, bias, S.h, r, c0);
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -272,7 +291,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         phase ^= 1;
         if (!ok) break;
         tc_fence_after();
-        hidden_epilogue(trow, bias + kHid, S.h, tid);
+        hidden_epilogue64(trow, bias + kHid, S.h, r, c0);
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -288,15 +307,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         tc_fence_after();
         float acc = 0.0f;
 #pragma unroll 1
-        for (int c = 0; c < kHid; c += 16) {
+        for (int c = c0; c < c0 + kHid / 2; c += 16) {
             float v[16];
             tmem_ld16(trow + (uint32_t)c, v);
 #pragma unroll
             for (int j = 0; j < 16; j++) acc = fmaf(gelu(v[j] + bias[2 * kHid + c + j]), bias[3 * kHid + c + j], acc);
         }
-        if (row < n) y[row] = acc + bias[4 * kHid];
+        if (half) S.part[r] = acc;
         tc_fence_before();
         __syncthreads();
+        if (!half && row < n) y[row] = acc + S.part[r] + bias[4 * kHid];
     }
     if (!ok && tid == 0) atomicOr(status, kStatusTimeout);
     tc_fence_before();
@@ -1054,7 +1074,7 @@ int ffg_mlp_forward(ffg_mlp* m, const uint16_t* x, size_t n, float* y) {
     if (!m || (n && (!x || !y))) return FFG_ERR_ARG;
     if (!n) return FFG_OK;
     if (((uintptr_t)x & 15) != 0) return mlp_err(m, FFG_ERR_ARG, "x must be 16-byte aligned");
-    mlp_forward_kernel<<<grid_rows(m, n), kThreads, sizeof(FwdSmem), m->stream>>>(
+    mlp_forward_kernel<<<grid_rows(m, n), kFwdThreads, sizeof(FwdSmem), m->stream>>>(
         m->img, reinterpret_cast<const __nv_bfloat16*>(x), n, y, m->status);
     MCK(cudaGetLastError());
     return mlp_check_status(m);
@@ -1146,7 +1166,7 @@ int ffg_mlp_set_targets(ffg_mlp* m, const uint16_t* x, size_t n, const double* c
     }
     if (!m->loss2) MCK(cudaMalloc(&m->loss2, 16));
     MCK(cudaMemsetAsync(m->loss2, 0, 16, m->stream));
-    mlp_forward_kernel<<<grid_rows(m, n), kThreads, sizeof(FwdSmem), m->stream>>>(
+    mlp_forward_kernel<<<grid_rows(m, n), kFwdThreads, sizeof(FwdSmem), m->stream>>>(
         m->img, reinterpret_cast<const __nv_bfloat16*>(x), n, m->ys, m->status);
     MCK(cudaGetLastError());
     segment_residual_kernel<<<(unsigned)nseg, 256, 0, m->stream>>>(m->ys, coef, seg, delta, m->R, m->loss2);
