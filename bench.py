@@ -527,6 +527,7 @@ def main_batched(args, rank, ws, local, dist):
         g, _ = h.adjoint(w)
         t_adj = time.perf_counter() - t1
         h.free()
+        step.emits = pr["emits"]
         return pr["apps"], pr["kernel_launches"], pr["seconds_total"], t_adj, expect, g
 
     for _ in range(args.warmup):
@@ -556,6 +557,8 @@ def main_batched(args, rank, ws, local, dist):
     value = allsum(dist, apps_tot) / t_max
     e2e = allsum(dist, apps_tot) / allmax(dist, sum(host_times))
     cpu = cpu_baseline(wl, tabs) if rank == 0 and not args.no_cpu_baseline else None
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm_peak = json.load(open(pk)).get("hbm_gbs", 6800.0) if os.path.exists(pk) else 6800.0
     if rank == 0:
         k = args.steps
         h2d = wl.keys.nbytes + wl.re.nbytes + wl.off.nbytes + wl.thetas.nbytes + tabs[0].nbytes
@@ -568,7 +571,14 @@ def main_batched(args, rank, ws, local, dist):
                            adjoint_ms=1e3 * adj_s / k, l2="flushed between steps (512 MB write)",
                            parallelism=f"replicas{ws}",
                            inputs="host arrays (the batched entry point copies them in each step)"),
-            "roofline": None,
+            "roofline": (lambda ab: {
+                "bound": "hbm", "achieved": ab / (t_max / k) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "frac": ab / (t_max / k) / 1e9 / hbm_peak, "traffic": None,
+                "kernel": "orbit engine forward + adjoint kernels", "launch_unit": "one step (forward + adjoint)",
+                "achieved_kind": "per-gate-equivalent of the forward pass (24 B x (2 x apps + emitted partners): "
+                                 "16 B one-word x/z key + 8 B coefficient) over the whole step, the adjoint's time "
+                                 "included; the engine keeps groups in shared memory and does not move these bytes",
+                "algorithmic_bytes_per_step": ab})(24.0 * (2 * apps_tot / k + step.emits)),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clk.summary(),
