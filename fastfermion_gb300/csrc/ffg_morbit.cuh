@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kBlock) morbit_classify(StoreView in, StoreVie
             sc.rep[i] = 0xffffffffu;
             const cplx c = load_coef<true>(in, i);
             apps += a.k;
-            if (!a.thr || !abs_le(c.re, c.im, a.tau)) out_append<KW, true>(out, oc, q, c);
+            out_append_warp<KW, true>(out, oc, q, c, !a.thr || !abs_le(c.re, c.im, a.tau));
             continue;
         }
 #pragma unroll
@@ -350,12 +350,12 @@ __device__ bool mgroup(const StoreView& in, const StoreView& out, const OrbitScr
     }
     const u32 cnt = *(volatile u32*)T.cnt;
     for (u32 m = rank; m < cnt; m += TEAM) {
-        if (!(T.st[m] & 1)) continue;
-        g_apps += (long long)a.k - T.since[m];
+        const bool live = (T.st[m] & 1) != 0;
+        if (live) g_apps += (long long)a.k - T.since[m];
         u64 k[KW];
 #pragma unroll
         for (int w = 0; w < KW; w++) k[w] = T.key[(u64)w * T.cap + m];
-        out_append<KW, true>(out, oc, k, cplx{T.re[m], T.im[m]});
+        out_append_warp<KW, true>(out, oc, k, cplx{T.re[m], T.im[m]}, live);
     }
     team_sync<TEAM>();
     apps += g_apps;
@@ -444,14 +444,14 @@ __global__ void __launch_bounds__(kBlock) morbit_single(StoreView in, StoreView 
         // created member from t + 1, survivors until the end of the run
         const bool kq = !a.thr || !abs_le(nq.re, nq.im, a.tau);
         apps += kq ? a.k : t + 1;
-        if (kq) out_append<KW, true>(out, oc, q0, nq);
+        out_append_warp<KW, true>(out, oc, q0, nq, kq);
         if (has_k) {
             const bool kk = !a.thr || !abs_le(nk.re, nk.im, a.tau);
             if (m0 == 2)
                 apps += kk ? a.k : t + 1;
             else if (kk)
                 apps += a.k - (t + 1);
-            if (kk) out_append<KW, true>(out, oc, k, nk);
+            out_append_warp<KW, true>(out, oc, k, nk, kk);
         }
     }
     long long tot = block_sum_ll(apps, sh);
