@@ -33,9 +33,11 @@ def test_learned_correction_gains_over_plain_w6():
     assert np.mean(errs[hard]) <= 0.1 * np.mean(base[hard])
     assert (errs <= 1e-3).sum() >= (base <= 1e-3).sum() + 3
     # the validated (largest) held-out error decides the path; above the bound
-    # the estimate is the judge's own run
+    # the estimate is a fresh run of the judge's propagation: the same terms,
+    # summed into <0|O|0> in the order the engine's atomic appends left them
+    # (the default, non-deterministic mode), so equal up to rounding
     v, _, path = sur.estimate(hdata[0].theta)
     if sur.held_out_error > sur.bound:
-        assert path == "fallback" and v == hdata[0].judge
+        assert path == "fallback" and abs(v - hdata[0].judge) <= 1e-13 * max(1.0, abs(v))
     else:
         assert path == "surrogate" and abs(v - hdata[0].judge) <= sur.bound
