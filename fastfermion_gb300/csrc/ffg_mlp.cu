@@ -75,9 +75,30 @@ constexpr uint32_t kIdescN32 = idesc_bf16(128, 32);
 // status bits of a launch
 constexpr int kStatusTimeout = 1;
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU in its tanh form (Hendrycks and Gimpel, "Gaussian Error Linear Units",
+// 2016):  gelu(z) = z/2 (1 + tanh(u)),  u = sqrt(2/pi) (z + 0.044715 z^3),
+// with tanh from the hardware approximation (tanh.approx.f32, one MUFU
+// instruction, relative error about 2^-11, below the BF16 rounding that
+// follows it).  gelu_grad is its exact derivative with the same tanh.
+constexpr float kGeluK = 0.7978845608028654f;     // sqrt(2/pi)
+constexpr float kGeluK3 = 0.035677408136300125f;  // 0.044715 sqrt(2/pi)
+constexpr float kGeluK3d = 0.10703222440890037f;  // 3 x 0.044715 sqrt(2/pi)
+
+__device__ __forceinline__ float tanh_approx(float u) {
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+    return t;
+}
+__device__ __forceinline__ float gelu(float z) {
+    const float u = z * fmaf(kGeluK3, z * z, kGeluK);
+    const float hz = 0.5f * z;
+    return fmaf(hz, tanh_approx(u), hz);
+}
 __device__ __forceinline__ float gelu_grad(float z) {
-    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+    const float z2 = z * z;
+    const float t = tanh_approx(z * fmaf(kGeluK3, z2, kGeluK));
+    // d/dz: (1 + t)/2 + z/2 (1 - t^2) sqrt(2/pi) (1 + 3 x 0.044715 z^2)
+    return fmaf(0.5f * z * fmaf(kGeluK3d, z2, kGeluK), fmaf(-t, t, 1.0f), 0.5f + 0.5f * t);
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -195,33 +216,120 @@ __global__ void __launch_bounds__(kThreads, 1)
 // ---------------------------------------------------------------------------
 // inference
 // ---------------------------------------------------------------------------
-// Inference runs 8 warps per CTA: warps w and w + 4 read the same TMEM lane
-// quarter (rows 32 (w % 4) ..) and split the 128 columns of every layer between
-// them, so the FP32 epilogue (bias, GELU, BF16 packing), which bounds this
-// kernel, has twice the warps and half the serial work per thread.
-constexpr int kFwdThreads = 256;
+// Inference keeps kFwdGroups tiles in flight per CTA, one per warpgroup of 128
+// threads.  Each warpgroup owns an activation image and 128 TMEM columns,
+// issues its own GEMMs and runs its own epilogues, meeting only its own warps
+// at named barriers; so while one warpgroup waits for its tile's MMAs, the
+// others run FP32 epilogues (bias, GELU, BF16 packing), which bound this
+// kernel.  A tile's input image sits at the start of its activation image: the
+// layer-1 epilogue overwrites it only after the layer-1 MMAs have read it.  The
+// weight images are loaded once per CTA and shared.  The epilogue runs on
+// pairs of columns with the packed FP32 instructions (add/mul/fma .f32x2,
+// round to nearest, as the scalar ones).
+constexpr int kFwdGroups = 4;
+constexpr int kFwdThreads = 128 * kFwdGroups;
+constexpr uint32_t kFwdTmemCols = kFwdGroups <= 2 ? 256 : 512;  // a power of two >= 128 x groups
+static_assert(kTile * kIn * 2 <= kTile * kHid * 2, "input image inside the activation image");
 
-// hidden-layer epilogue of one thread: bias + GELU of columns c0 .. c0+63 of
-// the accumulator row into the next layer's operand image
-__device__ __forceinline__ void hidden_epilogue64(uint32_t trow, const float* bias, uint8_t* img, int r, int c0) {
-#pragma unroll 1
-    for (int c = c0; c < c0 + kHid / 2; c += 16) {
-        float v[16];
-        tmem_ld16(trow + (uint32_t)c, v);
+struct __align__(1024) FwdSmem {
+    uint8_t w[kFwdImgBytes];                  // W1 | W2 | W3 images, bias block
+    uint8_t h[kFwdGroups][kTile * kHid * 2];  // input (K = 32), then hidden activation (K = 128) images
+    uint64_t bar_w;
+    uint64_t bar_mma[kFwdGroups];
+    uint32_t tmem;
+};
+
+// Barrier over the 128 threads of warpgroup g (ids 1..kFwdGroups; 0 is
+// __syncthreads), returning the AND of v over them.
+__device__ __forceinline__ bool group_sync_and(int g, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(g + 1)
+        : "memory");
+    return r != 0;
+}
+
+// 32 consecutive 32-bit TMEM columns of this thread's lane (one wait)
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int j = 0; j < 16; j++) v[j] = gelu(v[j] + bias[c + j]);
-        store_row16(img, r, c, kHid, v);
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// --- two FP32 values in one 64-bit register (low half first) -----------------
+__device__ __forceinline__ uint64_t f2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_split(uint64_t r, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// gelu of two values, the same operations (and results) as the scalar gelu
+__device__ __forceinline__ uint64_t gelu2(uint64_t z) {
+    const uint64_t u = mul2(z, fma2(f2(kGeluK3, kGeluK3), mul2(z, z), f2(kGeluK, kGeluK)));
+    float u0, u1;
+    f2_split(u, u0, u1);
+    const uint64_t hz = mul2(f2(0.5f, 0.5f), z);
+    return fma2(hz, f2(tanh_approx(u0), tanh_approx(u1)), hz);
+}
+
+// bias + GELU of 32 accumulator columns (v) with bias b[0..31], in pairs
+__device__ __forceinline__ void bias_gelu32(float (&v)[32], const float* b) {
+    const float4* b4 = reinterpret_cast<const float4*>(b);
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const float4 bb = b4[j];
+        const uint64_t h0 = gelu2(add2(f2(v[4 * j], v[4 * j + 1]), f2(bb.x, bb.y)));
+        const uint64_t h1 = gelu2(add2(f2(v[4 * j + 2], v[4 * j + 3]), f2(bb.z, bb.w)));
+        f2_split(h0, v[4 * j], v[4 * j + 1]);
+        f2_split(h1, v[4 * j + 2], v[4 * j + 3]);
     }
 }
 
-struct __align__(1024) FwdSmem {
-    uint8_t w[kFwdImgBytes];        // W1 | W2 | W3 images, bias block
-    uint8_t x[kTile * kIn * 2];     // input tile image (K = 32)
-    uint8_t h[kTile * kHid * 2];    // hidden activations image (K = 128)
-    float part[kTile];              // the second column half's share of each row's output
-    uint64_t bar_w, bar_mma;
-    uint32_t tmem;
-};
+// hidden-layer epilogue of one thread: bias + GELU of the 128 columns of its
+// accumulator row into the next layer's operand image
+__device__ __forceinline__ void hidden_epilogue(uint32_t trow, const float* bias, uint8_t* img, int r) {
+#pragma unroll 1
+    for (int c = 0; c < kHid; c += 32) {
+        float v[32];
+        tmem_ld32(trow + (uint32_t)c, v);
+        bias_gelu32(v, bias + c);
+        store_row16(img, r, c, kHid, *reinterpret_cast<const float(*)[16]>(&v[0]));
+        store_row16(img, r, c + 16, kHid, *reinterpret_cast<const float(*)[16]>(&v[16]));
+    }
+}
 
 __global__ void __launch_bounds__(kFwdThreads, 1)
     mlp_forward_kernel(const uint8_t* __restrict__ wimg, const __nv_bfloat16* __restrict__ x, size_t n,
@@ -229,20 +337,19 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     FwdSmem& S = *reinterpret_cast<FwdSmem*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int r = 32 * (warp & 3) + (tid & 31);  // row of the tile = TMEM lane
-    const int half = warp >> 2;                  // column half of this thread
-    const int c0 = half * (kHid / 2);
+    const int g = warp >> 2;                     // warpgroup = tile slot
+    const int r = tid & 127;                     // row of the tile = TMEM lane
     const size_t ntiles = (n + kTile - 1) / kTile;
     if (tid == 0) {
         mbar_init(&S.bar_w, 1);
-        mbar_init(&S.bar_mma, 1);
+        for (int i = 0; i < kFwdGroups; i++) mbar_init(&S.bar_mma[i], 1);
         mbar_fence_init();
     }
-    if (warp == 0) tmem_alloc(&S.tmem, 128);
+    if (warp == 0) tmem_alloc(&S.tmem, kFwdTmemCols);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = S.tmem;
+    const uint32_t tmem = S.tmem + (uint32_t)(128 * g);
     const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
     if (tid == 0) {
         mbar_expect_tx(&S.bar_w, kFwdImgBytes);
@@ -250,80 +357,68 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
     }
     bool ok = __syncthreads_and(mbar_wait(&S.bar_w, 0));
     const float* bias = reinterpret_cast<const float*>(S.w + kImgBias);
-    const uint32_t sx = smem_u32(S.x), sh = smem_u32(S.h);
+    uint8_t* himg = S.h[g];
+    const uint32_t sh = smem_u32(himg);
+    uint64_t* bar = &S.bar_mma[g];
+    const bool issuer = r == 0;
     uint32_t phase = 0;
-    for (size_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+    // one GEMM of this warpgroup's tile: issue, then wait for it (bounded)
+    auto gemm = [&](uint32_t a_s, uint32_t b_off, int K) {
+        if (issuer) {
+            tc_fence_after();
+            issue_gemm(tmem, a_s, smem_u32(S.w + b_off), K, kIdescN128);
+            mma_commit(bar);
+        }
+        const bool done = group_sync_and(g, mbar_wait(bar, phase));
+        phase ^= 1;
+        tc_fence_after();
+        return done;
+    };
+    auto operands_ready = [&]() {
+        fence_async_smem();
+        tc_fence_before();
+        group_sync_and(g, true);
+    };
+    for (size_t tile = (size_t)blockIdx.x * kFwdGroups + g; ok && tile < ntiles;
+         tile += (size_t)gridDim.x * kFwdGroups) {
         const size_t row = tile * kTile + r;
-        {  // each half stages two of the row's four 16-byte input chunks
-            uint4 v[2] = {};
-            if (row < n) {
-                const uint4* src = reinterpret_cast<const uint4*>(x + row * kIn) + 2 * half;
-                v[0] = __ldg(src);
-                v[1] = __ldg(src + 1);
-            }
-            *reinterpret_cast<uint4*>(S.x + img_off(r, 16 * half, kIn)) = v[0];
-            *reinterpret_cast<uint4*>(S.x + img_off(r, 16 * half + 8, kIn)) = v[1];
-        }
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-        // layer 1
-        if (tid == 0) {
-            tc_fence_after();
-            issue_gemm(tmem, sx, smem_u32(S.w + kImgW1), kIn, kIdescN128);
-            mma_commit(&S.bar_mma);
-        }
-        ok = __syncthreads_and(mbar_wait(&S.bar_mma, phase));
-        phase ^= 1;
-        if (!ok) break;
-        tc_fence_after();
-        hidden_epilogue64(trow, bias, S.h, r, c0);
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-        // layer 2
-        if (tid == 0) {
-            tc_fence_after();
-            issue_gemm(tmem, sh, smem_u32(S.w + kImgW2), kHid, kIdescN128);
-            mma_commit(&S.bar_mma);
-        }
-        ok = __syncthreads_and(mbar_wait(&S.bar_mma, phase));
-        phase ^= 1;
-        if (!ok) break;
-        tc_fence_after();
-        hidden_epilogue64(trow, bias + kHid, S.h, r, c0);
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
+        stage_x(himg, r, x, n, row);
+        operands_ready();
+        if (!(ok = gemm(sh, kImgW1, kIn))) break;
+        hidden_epilogue(trow, bias, himg, r);
+        operands_ready();
+        if (!(ok = gemm(sh, kImgW2, kHid))) break;
+        hidden_epilogue(trow, bias + kHid, himg, r);
+        operands_ready();
+        if (!(ok = gemm(sh, kImgW3, kHid))) break;
         // layer 3 and the output layer
-        if (tid == 0) {
-            tc_fence_after();
-            issue_gemm(tmem, sh, smem_u32(S.w + kImgW3), kHid, kIdescN128);
-            mma_commit(&S.bar_mma);
-        }
-        ok = __syncthreads_and(mbar_wait(&S.bar_mma, phase));
-        phase ^= 1;
-        if (!ok) break;
-        tc_fence_after();
-        float acc = 0.0f;
+        uint64_t acc = f2(0.0f, 0.0f);  // even and odd columns
 #pragma unroll 1
-        for (int c = c0; c < c0 + kHid / 2; c += 16) {
-            float v[16];
-            tmem_ld16(trow + (uint32_t)c, v);
+        for (int c = 0; c < kHid; c += 32) {
+            float v[32];
+            tmem_ld32(trow + (uint32_t)c, v);
+            bias_gelu32(v, bias + 2 * kHid + c);
+            const float4* w4 = reinterpret_cast<const float4*>(bias + 3 * kHid + c);
 #pragma unroll
-            for (int j = 0; j < 16; j++) acc = fmaf(gelu(v[j] + bias[2 * kHid + c + j]), bias[3 * kHid + c + j], acc);
+            for (int j = 0; j < 8; j++) {
+                const float4 w = w4[j];
+                acc = fma2(f2(v[4 * j], v[4 * j + 1]), f2(w.x, w.y), acc);
+                acc = fma2(f2(v[4 * j + 2], v[4 * j + 3]), f2(w.z, w.w), acc);
+            }
         }
-        if (half) S.part[r] = acc;
+        float acc0, acc1;
+        f2_split(acc, acc0, acc1);
+        if (row < n) y[row] = (acc0 + acc1) + bias[4 * kHid];
+        // this tile's TMEM reads are done before the next tile's first MMA
         tc_fence_before();
-        __syncthreads();
-        if (!half && row < n) y[row] = acc + S.part[r] + bias[4 * kHid];
+        group_sync_and(g, true);
     }
-    if (!ok && tid == 0) atomicOr(status, kStatusTimeout);
+    if (!ok && r == 0) atomicOr(status, kStatusTimeout);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
-        tmem_dealloc(tmem, 128);
+        tmem_dealloc(S.tmem, kFwdTmemCols);
     }
 }
 
@@ -960,6 +1055,12 @@ int grid_rows(const ffg_mlp* m, size_t n) {
     return (int)std::max<size_t>(1, std::min<size_t>(tiles, (size_t)m->num_sms));
 }
 
+// inference CTAs: kFwdGroups tiles at a time, at most one CTA per SM
+int grid_fwd(const ffg_mlp* m, size_t n) {
+    const size_t slots = (n + (size_t)kTile * kFwdGroups - 1) / ((size_t)kTile * kFwdGroups);
+    return (int)std::max<size_t>(1, std::min<size_t>(slots, (size_t)m->num_sms));
+}
+
 // forward and backward over n rows into m->grad (cleared first when clear)
 int run_gradient(ffg_mlp* m, const uint16_t* x, const float* target, const float* weight, size_t n,
                  float* y) {
@@ -1074,7 +1175,7 @@ int ffg_mlp_forward(ffg_mlp* m, const uint16_t* x, size_t n, float* y) {
     if (!m || (n && (!x || !y))) return FFG_ERR_ARG;
     if (!n) return FFG_OK;
     if (((uintptr_t)x & 15) != 0) return mlp_err(m, FFG_ERR_ARG, "x must be 16-byte aligned");
-    mlp_forward_kernel<<<grid_rows(m, n), kFwdThreads, sizeof(FwdSmem), m->stream>>>(
+    mlp_forward_kernel<<<grid_fwd(m, n), kFwdThreads, sizeof(FwdSmem), m->stream>>>(
         m->img, reinterpret_cast<const __nv_bfloat16*>(x), n, y, m->status);
     MCK(cudaGetLastError());
     return mlp_check_status(m);
@@ -1166,7 +1267,7 @@ int ffg_mlp_set_targets(ffg_mlp* m, const uint16_t* x, size_t n, const double* c
     }
     if (!m->loss2) MCK(cudaMalloc(&m->loss2, 16));
     MCK(cudaMemsetAsync(m->loss2, 0, 16, m->stream));
-    mlp_forward_kernel<<<grid_rows(m, n), kFwdThreads, sizeof(FwdSmem), m->stream>>>(
+    mlp_forward_kernel<<<grid_fwd(m, n), kFwdThreads, sizeof(FwdSmem), m->stream>>>(
         m->img, reinterpret_cast<const __nv_bfloat16*>(x), n, m->ys, m->status);
     MCK(cudaGetLastError());
     segment_residual_kernel<<<(unsigned)nseg, 256, 0, m->stream>>>(m->ys, coef, seg, delta, m->R, m->loss2);

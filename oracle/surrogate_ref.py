@@ -7,8 +7,11 @@ discards the partners that the degree filter drops
 (src/pauli/propagate.h:71-89); these functions restate the GPU's own
 definitions so that its kernels can be checked against them.
 
-Network: 32 -> 128 -> 128 -> 128 -> 1, GELU (exact, erf form) after each
-hidden layer.  The GPU rounds the GEMM operands to BF16 (round to nearest
+Network: 32 -> 128 -> 128 -> 128 -> 1, GELU after each hidden layer, in
+the tanh form of Hendrycks and Gimpel (2016):
+gelu(z) = z/2 (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))).  The GPU evaluates
+that tanh with its hardware approximation (relative error about 2^-11); here
+it is exact.  The GPU rounds the GEMM operands to BF16 (round to nearest
 even) -- the weights W1..W3, the input x, the hidden activations H1, H2 and
 the pre-activation gradients dZ1..dZ3 -- and accumulates in FP32; everything
 else is FP32.  `forward`/`gradient` reproduce those roundings (accumulating in
@@ -21,7 +24,6 @@ b2[128], W3[128][128], b3[128], w4[128], b4.
 import math
 
 import numpy as np
-from scipy.special import erf
 
 IN, HID = 32, 128
 NPARAMS = HID * IN + HID + 2 * (HID * HID + HID) + HID + 1
@@ -71,12 +73,17 @@ def init_params(seed=0):
     return pack(d).astype(np.float32)
 
 
+_GK = math.sqrt(2.0 / math.pi)
+_GA = 0.044715
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / math.sqrt(2.0)))
+    return 0.5 * z * (1.0 + np.tanh(_GK * (z + _GA * z * z * z)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    t = np.tanh(_GK * (z + _GA * z * z * z))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _GK * (1.0 + 3.0 * _GA * z * z)
 
 
 def _round(a, on):

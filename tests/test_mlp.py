@@ -3,11 +3,12 @@ the features of dropped partners, against the CPU restatement in
 oracle/surrogate_ref.py.
 
 Tolerances: the GPU and the restatement round the same GEMM operands to BF16
-and differ only in the order of FP32 sums (and in the last FP32 bit of
-erf/exp), which can move an activation across a BF16 rounding boundary
-(2^-8 relative).  Outputs and gradients are therefore compared with a
-norm-relative tolerance of 1e-2; the GEMM self-test, whose inputs are exact
-BF16 values, with 1e-5.
+and differ in the order of FP32 sums and in the GELU's tanh, which the GPU
+takes from its hardware approximation (relative error about 2^-11) and the
+restatement computes exactly.  Either can move an activation across a BF16
+rounding boundary (2^-8 relative).  Outputs and gradients are therefore
+compared with a norm-relative tolerance of 1e-2, the loss with 5e-3; the GEMM
+self-test, whose inputs are exact BF16 values, with 1e-5.
 """
 import numpy as np
 import pytest
@@ -94,7 +95,7 @@ def _problem(seed, n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n", [1, 127, 128, 300, 5000])
+@pytest.mark.parametrize("n", [1, 127, 128, 300, 5000, 150001])
 def test_forward_matches_restatement(mlp, n):
     import torch
     p, xb, _, _ = _problem(n, n)
@@ -116,7 +117,7 @@ def test_gradient_matches_restatement(mlp, n):
     x = _dev(torch, xb.view(np.int16))
     g, loss = mlp.gradient(x, _dev(torch, t), _dev(torch, w), n)
     want, wloss = R.gradient(p, R.from_bits(xb), t.astype(np.float64), w.astype(np.float64))
-    assert abs(loss - wloss) <= 1e-3 * abs(wloss)
+    assert abs(loss - wloss) <= 5e-3 * abs(wloss)
     o = 0
     for name, size in (("W1", 4096), ("b1", 128), ("W2", 16384), ("b2", 128), ("W3", 16384), ("b3", 128),
                        ("w4", 128), ("b4", 1)):
