@@ -537,18 +537,38 @@ struct OrbitTable {
     unsigned int flag;                    // the group outgrew the table
 };
 
+// Hash of a key for the per-group tables (one evaluation per member and gate,
+// so it is kept short): the key words are folded into 64 bits with a
+// different rotation per word (the x and z bits of one qubit land apart),
+// the high half is folded into the low one, and one multiplication by an odd
+// constant mixes it (multiplicative hashing).  Bits 32.. of the product, the
+// table position, depend on every bit of the fold; bits 13..31 serve as a
+// fingerprint.  A full key match is still required to find a member, so the
+// hash only decides where members sit in a table, never the results.
+__device__ __forceinline__ u64 rotl64(u64 x, int r) { return (x << r) | (x >> (64 - r)); }
+
+template <int KW>
+__device__ __forceinline__ u64 tab_hash(const u64* k) {
+    constexpr int rot[4] = {0, 32, 16, 48};
+    u64 x = k[0];
+#pragma unroll
+    for (int w = 1; w < KW; w++) x ^= rotl64(k[w], rot[w & 3]);
+    x ^= x >> 32;
+    return x * 0x9e3779b97f4a7c15ull;
+}
+__device__ __forceinline__ u32 tab_pos(u64 h) { return (u32)(h >> 32); }
+__device__ __forceinline__ u32 tab_fp(u64 h) { return (u32)h >> 13; }  // 19 bits
+
 template <int KW>
 __device__ __forceinline__ u32 small_hash(const u64* k) {
-    u64 h = mix64(k[0] ^ 0x2545f4914f6cdd1dull);
-#pragma unroll
-    for (int w = 1; w < KW; w++) h = mix64(h ^ k[w]);
-    return (u32)h;
+    return tab_pos(tab_hash<KW>(k));
 }
 
 // member index of key k or -1 (lanes of one warp share the table)
+// hp: small_hash of the key
 template <int KW, bool CPLX>
-__device__ __forceinline__ int table_find(const OrbitTable<KW, CPLX>& T, const u64* k) {
-    u32 pos = small_hash<KW>(k) & (2 * kOrbitCap - 1);
+__device__ __forceinline__ int table_find(const OrbitTable<KW, CPLX>& T, const u64* k, u32 hp) {
+    u32 pos = hp & (2 * kOrbitCap - 1);
     for (int probe = 0; probe < 2 * kOrbitCap; probe++) {
         const unsigned short m = ((volatile unsigned short*)T.slot)[pos];
         if (m == 0xffff) return -1;
@@ -562,8 +582,8 @@ __device__ __forceinline__ int table_find(const OrbitTable<KW, CPLX>& T, const u
 }
 
 template <int KW, bool CPLX>
-__device__ __forceinline__ void table_insert(OrbitTable<KW, CPLX>& T, const u64* k, unsigned short m) {
-    u32 pos = small_hash<KW>(k) & (2 * kOrbitCap - 1);
+__device__ __forceinline__ void table_insert(OrbitTable<KW, CPLX>& T, u32 hp, unsigned short m) {
+    u32 pos = hp & (2 * kOrbitCap - 1);
     for (int probe = 0; probe < 2 * kOrbitCap; probe++) {
         unsigned int* word = (unsigned int*)&T.slot[pos & ~1u];
         const int hi = pos & 1;
@@ -620,7 +640,7 @@ __global__ void __launch_bounds__(32 * kOrbitWarps, 4) orbit_process(StoreView i
             for (int w = 0; w < KW; w++) T.key[m][w] = sc.gkey[(u64)w * sc.cap_in + pm];
             T.re[m] = sc.gcoef[pm];
             if (CPLX) T.im[m] = sc.gcoef[sc.cap_in + pm];
-            table_insert<KW, CPLX>(T, T.key[m], (unsigned short)m);
+            table_insert<KW, CPLX>(T, small_hash<KW>(T.key[m]), (unsigned short)m);
         }
         if (lane == 0) {
             T.cnt = m0;
@@ -665,7 +685,8 @@ __global__ void __launch_bounds__(32 * kOrbitWarps, 4) orbit_process(StoreView i
                     const int jQ = G.yP + yQ + 2 * zxQ - yK;  // P*Q -> K
                     const int jK = G.yP + yK + 2 * zxK - yQ;  // P*K -> Q
                     const cplx ci = {T.re[m], CPLX ? T.im[m] : 0.0};
-                    const int j = table_find<KW, CPLX>(T, k);
+                    const u32 hk = small_hash<KW>(k);
+                    const int j = table_find<KW, CPLX>(T, k, hk);
                     if (j >= 0 && j < cnt0) {
                         if (j < m) continue;  // the pair belongs to member j
                         const cplx cj = {T.re[j], CPLX ? T.im[j] : 0.0};
@@ -699,7 +720,7 @@ __global__ void __launch_bounds__(32 * kOrbitWarps, 4) orbit_process(StoreView i
                                 T.re[idx] = nv.re;
                                 if (CPLX) T.im[idx] = nv.im;
                                 __threadfence_block();
-                                table_insert<KW, CPLX>(T, k, (unsigned short)idx);
+                                table_insert<KW, CPLX>(T, hk, (unsigned short)idx);
                                 g_created++;
                                 g_xapps += a.k - 1 - t;
                             }
@@ -796,31 +817,43 @@ __device__ __forceinline__ T tld(const T* p) {
     return __ldcg(p);
 }
 
-template <int KW, bool CPLX, bool SM = false>
-__device__ __forceinline__ int big_find(const BigRegion<KW, CPLX>& G, u32 rcap, const u64* k) {
+// Block-level tables in shared memory (FP) keep a fingerprint with each
+// member index, (tab_fp << 12) | index (tables of at most 4096 members, the
+// top bit never set), so that a probe reads the member's key only when the
+// fingerprints agree; global-memory regions (any size) keep the index alone.
+// Both take the key's tab_hash h.
+constexpr u32 kFpShift = 12;
+
+template <int KW, bool CPLX, bool SM = false, bool FP = false>
+__device__ __forceinline__ int big_find(const BigRegion<KW, CPLX>& G, u32 rcap, const u64* k, u64 h) {
     const u32 mask = 2 * rcap - 1;
-    u32 pos = small_hash<KW>(k) & mask;
+    u32 pos = tab_pos(h) & mask;
+    const u32 fp = tab_fp(h);
     for (u32 probe = 0; probe <= mask; probe++) {
-        const u32 m = tld<SM>(&G.slot[pos]);
-        if (m == 0xffffffffu) return -1;
+        const u32 e = tld<SM>(&G.slot[pos]);
+        if (e == 0xffffffffu) return -1;
+        if (!FP || (e >> kFpShift) == fp) {
+            const u32 m = FP ? (e & ((1u << kFpShift) - 1)) : e;
 #ifdef FFG_ORBIT_CHECK
-        if (m >= rcap) return (int)0x7fffffff;
+            if (m >= rcap) return (int)0x7fffffff;
 #endif
-        bool eq = true;
+            bool eq = true;
 #pragma unroll
-        for (int w = 0; w < KW; w++) eq = eq && tld<SM>(&G.key[(u64)w * rcap + m]) == k[w];
-        if (eq) return (int)m;
+            for (int w = 0; w < KW; w++) eq = eq && tld<SM>(&G.key[(u64)w * rcap + m]) == k[w];
+            if (eq) return (int)m;
+        }
         pos = (pos + 1) & mask;
     }
     return -1;
 }
 
-template <int KW, bool CPLX>
-__device__ __forceinline__ void big_insert(const BigRegion<KW, CPLX>& G, u32 rcap, const u64* k, u32 m) {
+template <int KW, bool CPLX, bool FP = false>
+__device__ __forceinline__ void big_insert(const BigRegion<KW, CPLX>& G, u32 rcap, u32 m, u64 h) {
     const u32 mask = 2 * rcap - 1;
-    u32 pos = small_hash<KW>(k) & mask;
+    u32 pos = tab_pos(h) & mask;
+    const u32 e = FP ? ((tab_fp(h) << kFpShift) | m) : m;
     for (u32 probe = 0; probe <= mask; probe++) {
-        if (atomicCAS(&G.slot[pos], 0xffffffffu, m) == 0xffffffffu) return;
+        if (atomicCAS(&G.slot[pos], 0xffffffffu, e) == 0xffffffffu) return;
         pos = (pos + 1) & mask;
     }
 }
@@ -833,6 +866,84 @@ constexpr size_t block_table_bytes() {
     return (size_t)KW * CAP * 8 + CAP * 8 * (CPLX ? 2 : 1) + 2 * CAP * 4 + 16;
 }
 
+// One member of a block-level group at gate t of the batch: pairs it with its
+// partner K = Q * P_t when K is a member that existed before the gate (the
+// lower index of the two does the update), or creates K (index cnt0 + the
+// gate's creation count *ctr) when the degree filter admits it; the
+// reference's arithmetic, filter and creation rule (src/pauli/propagate.h:71-89).
+template <int NW, bool CPLX, bool SM, bool REC>
+__device__ __forceinline__ void big_member(const BigRegion<2 * NW, CPLX>& G, u32 rcap, u32 m, u32 cnt0, int t,
+                                           const BatchGate& Gt, double gc, double gs, const OrbitBatchArgs& a,
+                                           u32* ctr, u32& g_emits, u32& g_created, u32& g_xapps) {
+    constexpr int KW = 2 * NW;
+    u64 q[KW], k[KW];
+#pragma unroll
+    for (int w = 0; w < KW; w++) {
+        q[w] = tld<SM>(&G.key[(u64)w * rcap + m]);
+        k[w] = q[w] ^ Gt.p[w];
+    }
+    int yQ = 0, yK = 0, zxQ = 0, zxK = 0, dQ = 0, dK = 0;
+#pragma unroll
+    for (int w = 0; w < NW; w++) {
+        yQ += __popcll(q[w] & q[NW + w]);
+        yK += __popcll(k[w] & k[NW + w]);
+        zxQ += __popcll(Gt.p[NW + w] & q[w]);
+        zxK += __popcll(Gt.p[NW + w] & k[w]);
+        dQ += __popcll(q[w] | q[NW + w]);
+        dK += __popcll(k[w] | k[NW + w]);
+    }
+    const int jQ = Gt.yP + yQ + 2 * zxQ - yK;
+    const int jK = Gt.yP + yK + 2 * zxK - yQ;
+    const cplx ci = {tld<SM>(&G.re[m]), CPLX ? tld<SM>(&G.im[m]) : 0.0};
+    const u64 hk = tab_hash<KW>(k);
+    const int j = big_find<KW, CPLX, SM, SM>(G, rcap, k, hk);
+    if (j >= 0 && (u32)j < cnt0) {
+        if ((u32)j < m) return;
+        const cplx cj = {tld<SM>(&G.re[j]), CPLX ? tld<SM>(&G.im[j]) : 0.0};
+        cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
+        if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
+        else if (REC && a.cap && dQ <= a.cap->maxdeg)
+            capture_drop<NW, CPLX>(*a.cap, q, rot_partner<CPLX>(cj, gs, jK), Gt.gidx);
+        if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
+        else if (REC && a.cap && dK <= a.cap->maxdeg)
+            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
+        g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
+        G.re[m] = ni.re;
+        G.re[j] = nj.re;
+        if (CPLX) {
+            G.im[m] = ni.im;
+            G.im[j] = nj.im;
+        }
+    } else {
+        const cplx ni = rot_keep<CPLX>(ci, gc);
+        G.re[m] = ni.re;
+        if (CPLX) G.im[m] = ni.im;
+        if (dK <= a.maxdeg) {
+            g_emits++;
+            const cplx nv = rot_add<CPLX>({0.0, 0.0}, rot_partner<CPLX>(ci, gs, jQ));
+            const u32 idx = cnt0 + atomicAdd(ctr, 1u);
+            if (idx >= rcap) {
+                atomicExch(G.flag, 1u);
+            } else {
+#pragma unroll
+                for (int w = 0; w < KW; w++) G.key[(u64)w * rcap + idx] = k[w];
+                G.re[idx] = nv.re;
+                if (CPLX) G.im[idx] = nv.im;
+                __threadfence_block();
+                big_insert<KW, CPLX, SM>(G, rcap, idx, hk);
+                g_created++;
+                g_xapps += a.k - 1 - t;
+            }
+        } else if (REC && a.cap && dK <= a.cap->maxdeg) {
+            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
+        }
+    }
+}
+
+// Groups that start with at most this many members are first run by one warp
+// of the block (see orbit_process_big).
+constexpr u32 kWarpPhase = 64;
+
 // Block-level group processing with TB threads per block.  SM: the table lives
 // in dynamic shared memory (CAP members); otherwise in the block's
 // global-memory region of bp.
@@ -842,7 +953,10 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                                                           const u32* list, u32 nlist, const u32* nlist_dev) {
     wait_prior_grid();
     constexpr int KW = 2 * NW;
+    static_assert(!SM || CAP <= (1u << kFpShift), "member indexes of a shared-memory table fit beside the fingerprint");
     __shared__ long long red[3][32];
+    __shared__ u32 big_cr[3];    // members created by a gate (ring of three)
+    __shared__ u32 big_done[2];  // gates applied and members after the warp phase
     extern __shared__ __align__(16) unsigned char btab[];
     if (*(volatile u32*)&oc->skip) return;
     if (nlist_dev) nlist = *(volatile const u32*)nlist_dev;  // list length written by an earlier kernel
@@ -876,6 +990,7 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
         if (threadIdx.x == 0) {
             *G.cnt = m0;
             *G.flag = m0 > rcap ? 1u : 0u;
+            big_cr[0] = 0;
         }
         __syncthreads();
         if (*(volatile u32*)G.flag) {
@@ -896,93 +1011,74 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
             G.re[m] = sc.gcoef[pm];
             if (CPLX) G.im[m] = sc.gcoef[sc.cap_in + pm];
             __threadfence_block();
-            big_insert<KW, CPLX>(G, rcap, k, m);
+            big_insert<KW, CPLX, SM>(G, rcap, m, tab_hash<KW>(k));
         }
         __syncthreads();
-        long long g_emits = 0, g_created = 0, g_xapps = 0;
-        bool stop = false;
+        u32 g_emits = 0, g_created = 0, g_xapps = 0;  // this thread, this group
         const u32 inst = group_instance(in, a, rep);
-        for (int wd = 0; wd < kAW && !stop; wd++) {
-            u64 bits = sc.amask[(u64)wd * sc.cap_in + rep];
-            while (bits && !stop) {
-                const int t = 64 * wd + __ffsll((long long)bits) - 1;
-                bits &= bits - 1;
-                const BatchGate Gt = a.gates[t];
-                double gc, gs;
-                gate_cs(a, Gt, t, inst, gc, gs);
-                u64 P[KW];
-#pragma unroll
-                for (int w = 0; w < KW; w++) P[w] = Gt.p[w];
-                const u32 cnt0 = *(volatile u32*)G.cnt;
-                __syncthreads();
-                for (u32 m = threadIdx.x; m < cnt0; m += blockDim.x) {
-                    OCHK(m < rcap, 4, m, cnt0, t)
-                    OCHK(t < a.k, 5, t, a.k, rep)
-                    u64 q[KW], k[KW];
-#pragma unroll
-                    for (int w = 0; w < KW; w++) {
-                        q[w] = tld<SM>(&G.key[(u64)w * rcap + m]);
-                        k[w] = q[w] ^ P[w];
+        const u64* A = sc.amask + rep;  // word w of the group's gate set at A[w * cap_in]
+        u32 cnt0 = m0;   // members before the current gate (the same in every thread)
+        int done = 0;    // gates of A applied so far
+        // Warp phase: while the group has at most kWarpPhase members, warp 0
+        // alone applies the gates (warp barriers only); the block's other warps
+        // wait at one block barrier.
+        if (SM && cnt0 <= kWarpPhase) {
+            if (threadIdx.x < 32) {
+                const int lane = threadIdx.x;
+                int gi = 0;
+                for (int wd = 0; wd < kAW && cnt0 <= kWarpPhase; wd++) {
+                    u64 bits = A[(u64)wd * sc.cap_in];
+                    while (bits && cnt0 <= kWarpPhase) {
+                        const int t = 64 * wd + __ffsll((long long)bits) - 1;
+                        bits &= bits - 1;
+                        u32* ctr = &big_cr[gi % 3];
+                        if (lane == 0) big_cr[(gi + 1) % 3] = 0;
+                        const BatchGate Gt = a.gates[t];
+                        double gc, gs;
+                        gate_cs(a, Gt, t, inst, gc, gs);
+                        for (u32 m = lane; m < cnt0; m += 32)
+                            big_member<NW, CPLX, SM, REC>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits,
+                                                           g_created, g_xapps);
+                        __syncwarp();
+                        cnt0 += *(volatile u32*)ctr;
+                        gi++;
+                        if (*(volatile u32*)G.flag) break;
                     }
-                    int yQ = 0, yK = 0, zxQ = 0, zxK = 0, dQ = 0, dK = 0;
-#pragma unroll
-                    for (int w = 0; w < NW; w++) {
-                        yQ += __popcll(q[w] & q[NW + w]);
-                        yK += __popcll(k[w] & k[NW + w]);
-                        zxQ += __popcll(P[NW + w] & q[w]);
-                        zxK += __popcll(P[NW + w] & k[w]);
-                        dQ += __popcll(q[w] | q[NW + w]);
-                        dK += __popcll(k[w] | k[NW + w]);
-                    }
-                    const int jQ = Gt.yP + yQ + 2 * zxQ - yK;
-                    const int jK = Gt.yP + yK + 2 * zxK - yQ;
-                    const cplx ci = {tld<SM>(&G.re[m]), CPLX ? tld<SM>(&G.im[m]) : 0.0};
-                    const int j = big_find<KW, CPLX, SM>(G, rcap, k);
-                    OCHK(j < (int)rcap, 6, j, rcap, m)
-                    if (j >= 0 && (u32)j < cnt0) {
-                        if ((u32)j < m) continue;
-                        const cplx cj = {tld<SM>(&G.re[j]), CPLX ? tld<SM>(&G.im[j]) : 0.0};
-                        cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
-                        if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
-                        else if (REC && a.cap && dQ <= a.cap->maxdeg)
-                            capture_drop<NW, CPLX>(*a.cap, q, rot_partner<CPLX>(cj, gs, jK), Gt.gidx);
-                        if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
-                        else if (REC && a.cap && dK <= a.cap->maxdeg)
-                            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
-                        g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
-                        G.re[m] = ni.re;
-                        G.re[j] = nj.re;
-                        if (CPLX) {
-                            G.im[m] = ni.im;
-                            G.im[j] = nj.im;
-                        }
-                    } else {
-                        const cplx ni = rot_keep<CPLX>(ci, gc);
-                        G.re[m] = ni.re;
-                        if (CPLX) G.im[m] = ni.im;
-                        if (dK <= a.maxdeg) {
-                            g_emits++;
-                            const cplx nv = rot_add<CPLX>({0.0, 0.0}, rot_partner<CPLX>(ci, gs, jQ));
-                            const u32 idx = atomicAdd(G.cnt, 1u);
-                            if (idx >= rcap) {
-                                atomicExch(G.flag, 1u);
-                            } else {
-#pragma unroll
-                                for (int w = 0; w < KW; w++) G.key[(u64)w * rcap + idx] = k[w];
-                                G.re[idx] = nv.re;
-                                if (CPLX) G.im[idx] = nv.im;
-                                __threadfence_block();
-                                big_insert<KW, CPLX>(G, rcap, k, idx);
-                                g_created++;
-                                g_xapps += a.k - 1 - t;
-                            }
-                        } else if (REC && a.cap && dK <= a.cap->maxdeg) {
-                            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
-                        }
-                    }
+                    if (*(volatile u32*)G.flag) break;
                 }
-                __syncthreads();
-                stop = *(volatile u32*)G.flag != 0;
+                if (lane == 0) {
+                    big_done[0] = (u32)gi;
+                    big_done[1] = cnt0;
+                }
+            }
+            __syncthreads();
+            done = (int)big_done[0];
+            cnt0 = big_done[1];
+        }
+        // Block phase: every thread, one block barrier per gate.  Creations of
+        // gate i count in big_cr[i % 3]; the slot of gate i + 1 is cleared
+        // during gate i (its last readers passed the barrier of gate i - 1).
+        {
+            int gi = 0;
+            bool stop = *(volatile u32*)G.flag != 0;
+            for (int wd = 0; wd < kAW && !stop; wd++) {
+                u64 bits = A[(u64)wd * sc.cap_in];
+                while (bits && !stop) {
+                    const int t = 64 * wd + __ffsll((long long)bits) - 1;
+                    bits &= bits - 1;
+                    if (gi++ < done) continue;
+                    u32* ctr = &big_cr[(gi - 1) % 3];
+                    if (threadIdx.x == 0) big_cr[gi % 3] = 0;
+                    const BatchGate Gt = a.gates[t];
+                    double gc, gs;
+                    gate_cs(a, Gt, t, inst, gc, gs);
+                    for (u32 m = threadIdx.x; m < cnt0; m += blockDim.x)
+                        big_member<NW, CPLX, SM, REC>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits, g_created,
+                                                       g_xapps);
+                    __syncthreads();
+                    cnt0 += *(volatile u32*)ctr;
+                    stop = *(volatile u32*)G.flag != 0;
+                }
             }
         }
         __syncthreads();
@@ -994,7 +1090,7 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
         emits += g_emits;
         created += g_created;
         xapps += g_xapps;
-        const u32 cnt = *(volatile u32*)G.cnt;
+        const u32 cnt = cnt0;
         if (threadIdx.x == 0) {
             atomicMax(&oc->max_members, cnt);
             atomicAdd(&oc->hist[31 - __clz(cnt | 1)], 1u);
