@@ -207,7 +207,7 @@ __device__ bool adj_group(const StoreView& in, const OrbitScratch& sc, const Adj
                     T.c[m] = rot_keep<false>(ci, gc).re;
                     if (dK <= a.maxdeg) {
                         const cplx nv = rot_add<false>({0.0, 0.0}, rot_partner<false>(ci, gs, jQ));
-                        const u32 idx = atomicAdd(T.cnt, 1u);
+                        const u32 idx = warp_reserve(T.cnt);
                         if (idx >= T.cap) {
                             atomicExch(T.flag, 1u);
                         } else {

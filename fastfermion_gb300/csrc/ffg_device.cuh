@@ -204,6 +204,27 @@ __device__ __forceinline__ cplx rot_add(cplx a, cplx b) {
     return {__dadd_rn(a.re, b.re), 0.0};
 }
 
+// The partner value when |s| = 1 (sin theta = +-1, e.g. RZZ(-pi/2)), real
+// mode: b*s is exact, so the product is b with its sign flipped when s < 0,
+// then the sign of i^j as in rot_partner -- the same value with no FP64
+// instruction (GB300 issues FP64 at a small fraction of the FP32 rate).
+template <bool CPLX>
+__device__ __forceinline__ cplx rot_partner_unit(cplx b, double s, int j) {
+    if (CPLX) return rot_partner<true>(b, s, j);
+    if (!(j & 1)) return {0.0, 0.0};
+    const bool neg = (s < 0.0) != ((j & 3) == 1);
+    return {__longlong_as_double(__double_as_longlong(b.re) ^ (neg ? (long long)0x8000000000000000ull : 0ll)), 0.0};
+}
+
+// The value of a new entry, 0 + v (the reference adds a partner into a
+// value-initialised coefficient): in real mode (finite v) that is v with a
+// negative zero made positive, without an FP64 addition.
+template <bool CPLX>
+__device__ __forceinline__ cplx rot_new(cplx v) {
+    if (CPLX) return rot_add<true>({0.0, 0.0}, v);
+    return {__double_as_longlong(v.re) == (long long)0x8000000000000000ull ? 0.0 : v.re, 0.0};
+}
+
 // ---------------------------------------------------------------------------
 // Truncation predicate |c| <= tau with |c| = hypot(re, im) correctly rounded
 // (the reference uses std::abs on std::complex<double>, i.e. libm hypot).

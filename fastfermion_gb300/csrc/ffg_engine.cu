@@ -923,10 +923,12 @@ struct Engine {
             // sc.big -> retry_list (count nretry[0]) -> sc.big (count nretry[1])
             bp.retry = retry_list;
             bp.nretry = nretry;
+            bp.fetch = &oc->fetch[0];
             CK(launch_k(ctx->pdl, team_k, ctx->num_sms * team_per_sm, tthreads, tt, ctx->stream, in, out, sc, oc, a,
                         bp, (const u32*)sc.big, 0u, nbig_dev));
             bp.retry = sc.big;
             bp.nretry = nretry + 1;
+            bp.fetch = &oc->fetch[1];
             CK(launch_k(ctx->pdl, block_k, ctx->num_sms, bthreads, tb, ctx->stream, in, out, sc, oc, a, bp,
                         (const u32*)retry_list, 0u, (const u32*)nretry));
             ctx->prof.kernel_launches += 2;
@@ -934,6 +936,7 @@ struct Engine {
             // sc.big -> retry_list (count nretry[1])
             bp.retry = retry_list;
             bp.nretry = nretry + 1;
+            bp.fetch = &oc->fetch[1];
             CK(launch_k(ctx->pdl, block_k, ctx->num_sms, bthreads, tb, ctx->stream, in, out, sc, oc, a, bp,
                         (const u32*)sc.big, 0u, nbig_dev));
             ctx->prof.kernel_launches++;

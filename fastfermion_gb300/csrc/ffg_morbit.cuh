@@ -307,7 +307,7 @@ __device__ bool mgroup(const StoreView& in, const StoreView& out, const OrbitScr
                             T.im[j] = nv.im;
                             T.st[j] = 2;
                         } else {
-                            const u32 idx = atomicAdd(T.cnt, 1u);
+                            const u32 idx = warp_reserve(T.cnt);
                             if (idx >= T.cap) {
                                 atomicExch(T.flag, 1u);
                             } else {

@@ -89,6 +89,8 @@ struct OrbitCounters {
     u32 nrest2;        // groups left by a sub-warp pass (list in OrbitScratch::list2)
     u64 n_in;          // terms entering the batch (set by orbit_gate)
     u64 gmask;         // group-index slots - 1 for this batch (set by orbit_gate)
+    u32 fetch[2];      // groups handed out by the team and block passes beyond their first round
+    u32 pad;
 };
 
 #ifdef FFG_ORBIT_CHECK
@@ -283,6 +285,21 @@ __device__ __forceinline__ void out_append_warp(const StoreView& o, OrbitCounter
     o.re[pos] = c.re;
     if (CPLX) o.im[pos] = c.im;
     o.dead[pos] = 0;
+}
+
+// Reserves one slot of the counter *ctr for each calling lane, with one atomic
+// per set of converged lanes that name the same counter (a group's new members
+// are numbered this way: a same-address atomic per lane serialises every
+// creating thread of a gate; lanes of one warp may serve different groups);
+// returns this lane's slot.
+__device__ __forceinline__ u32 warp_reserve(u32* ctr) {
+    const unsigned mask = __match_any_sync(__activemask(), (unsigned long long)ctr);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    u32 base = 0;
+    if (lane == leader) base = atomicAdd(ctr, (u32)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    return base + (u32)__popc(mask & ((1u << lane) - 1u));
 }
 
 template <int KW, bool CPLX>
@@ -660,6 +677,10 @@ __global__ void __launch_bounds__(32 * kOrbitWarps, 4) orbit_process(StoreView i
                 const BatchGate G = a.gates[t];
                 double gc, gs;
                 gate_cs(a, G, t, inst, gc, gs);
+                const bool unit = !CPLX && (gs == 1.0 || gs == -1.0);
+                auto partner = [&](cplx b, int jj) {
+                    return unit ? rot_partner_unit<CPLX>(b, gs, jj) : rot_partner<CPLX>(b, gs, jj);
+                };
                 u64 P[KW];
 #pragma unroll
                 for (int w = 0; w < KW; w++) P[w] = G.p[w];
@@ -691,12 +712,12 @@ __global__ void __launch_bounds__(32 * kOrbitWarps, 4) orbit_process(StoreView i
                         if (j < m) continue;  // the pair belongs to member j
                         const cplx cj = {T.re[j], CPLX ? T.im[j] : 0.0};
                         cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
-                        if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
+                        if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, partner(cj, jK));
                         else if (REC && a.cap && dQ <= a.cap->maxdeg)
-                            capture_drop<NW, CPLX>(*a.cap, q, rot_partner<CPLX>(cj, gs, jK), G.gidx);
-                        if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
+                            capture_drop<NW, CPLX>(*a.cap, q, partner(cj, jK), G.gidx);
+                        if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, partner(ci, jQ));
                         else if (REC && a.cap && dK <= a.cap->maxdeg)
-                            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), G.gidx);
+                            capture_drop<NW, CPLX>(*a.cap, k, partner(ci, jQ), G.gidx);
                         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
                         T.re[m] = ni.re;
                         T.re[j] = nj.re;
@@ -710,8 +731,8 @@ __global__ void __launch_bounds__(32 * kOrbitWarps, 4) orbit_process(StoreView i
                         if (CPLX) T.im[m] = ni.im;
                         if (dK <= a.maxdeg) {
                             g_emits++;
-                            const cplx nv = rot_add<CPLX>({0.0, 0.0}, rot_partner<CPLX>(ci, gs, jQ));
-                            const unsigned int idx = atomicAdd(&T.cnt, 1u);
+                            const cplx nv = rot_new<CPLX>(partner(ci, jQ));
+                            const unsigned int idx = warp_reserve(&T.cnt);
                             if (idx >= (unsigned int)kOrbitCap) {
                                 atomicExch(&T.flag, 1u);
                             } else {
@@ -725,7 +746,7 @@ __global__ void __launch_bounds__(32 * kOrbitWarps, 4) orbit_process(StoreView i
                                 g_xapps += a.k - 1 - t;
                             }
                         } else if (REC && a.cap && dK <= a.cap->maxdeg) {
-                            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), G.gidx);
+                            capture_drop<NW, CPLX>(*a.cap, k, partner(ci, jQ), G.gidx);
                         }
                     }
                 }
@@ -780,6 +801,7 @@ struct BigPool {
     u32 rcap;        // members per region (power of two)
     u32* retry;      // representatives of groups that outgrew their region
     u32* nretry;
+    u32* fetch;      // counter of groups handed out after each block's first (null: blocks stride the list)
 };
 
 template <int KW, bool CPLX>
@@ -873,9 +895,13 @@ constexpr size_t block_table_bytes() {
 // reference's arithmetic, filter and creation rule (src/pauli/propagate.h:71-89).
 template <int NW, bool CPLX, bool SM, bool REC>
 __device__ __forceinline__ void big_member(const BigRegion<2 * NW, CPLX>& G, u32 rcap, u32 m, u32 cnt0, int t,
-                                           const BatchGate& Gt, double gc, double gs, const OrbitBatchArgs& a,
-                                           u32* ctr, u32& g_emits, u32& g_created, u32& g_xapps) {
+                                           const BatchGate& Gt, double gc, double gs, bool unit,
+                                           const OrbitBatchArgs& a, u32* ctr, u32& g_emits, u32& g_created,
+                                           u32& g_xapps) {
     constexpr int KW = 2 * NW;
+    auto partner = [&](cplx b, int j) {
+        return unit ? rot_partner_unit<CPLX>(b, gs, j) : rot_partner<CPLX>(b, gs, j);
+    };
     u64 q[KW], k[KW];
 #pragma unroll
     for (int w = 0; w < KW; w++) {
@@ -901,12 +927,12 @@ __device__ __forceinline__ void big_member(const BigRegion<2 * NW, CPLX>& G, u32
         if ((u32)j < m) return;
         const cplx cj = {tld<SM>(&G.re[j]), CPLX ? tld<SM>(&G.im[j]) : 0.0};
         cplx ni = rot_keep<CPLX>(ci, gc), nj = rot_keep<CPLX>(cj, gc);
-        if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, rot_partner<CPLX>(cj, gs, jK));
+        if (dQ <= a.maxdeg) ni = rot_add<CPLX>(ni, partner(cj, jK));
         else if (REC && a.cap && dQ <= a.cap->maxdeg)
-            capture_drop<NW, CPLX>(*a.cap, q, rot_partner<CPLX>(cj, gs, jK), Gt.gidx);
-        if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, rot_partner<CPLX>(ci, gs, jQ));
+            capture_drop<NW, CPLX>(*a.cap, q, partner(cj, jK), Gt.gidx);
+        if (dK <= a.maxdeg) nj = rot_add<CPLX>(nj, partner(ci, jQ));
         else if (REC && a.cap && dK <= a.cap->maxdeg)
-            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
+            capture_drop<NW, CPLX>(*a.cap, k, partner(ci, jQ), Gt.gidx);
         g_emits += (dQ <= a.maxdeg) + (dK <= a.maxdeg);
         G.re[m] = ni.re;
         G.re[j] = nj.re;
@@ -920,8 +946,8 @@ __device__ __forceinline__ void big_member(const BigRegion<2 * NW, CPLX>& G, u32
         if (CPLX) G.im[m] = ni.im;
         if (dK <= a.maxdeg) {
             g_emits++;
-            const cplx nv = rot_add<CPLX>({0.0, 0.0}, rot_partner<CPLX>(ci, gs, jQ));
-            const u32 idx = cnt0 + atomicAdd(ctr, 1u);
+            const cplx nv = rot_new<CPLX>(partner(ci, jQ));
+            const u32 idx = cnt0 + warp_reserve(ctr);
             if (idx >= rcap) {
                 atomicExch(G.flag, 1u);
             } else {
@@ -935,7 +961,7 @@ __device__ __forceinline__ void big_member(const BigRegion<2 * NW, CPLX>& G, u32
                 g_xapps += a.k - 1 - t;
             }
         } else if (REC && a.cap && dK <= a.cap->maxdeg) {
-            capture_drop<NW, CPLX>(*a.cap, k, rot_partner<CPLX>(ci, gs, jQ), Gt.gidx);
+            capture_drop<NW, CPLX>(*a.cap, k, partner(ci, jQ), Gt.gidx);
         }
     }
 }
@@ -961,7 +987,17 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
     if (*(volatile u32*)&oc->skip) return;
     if (nlist_dev) nlist = *(volatile const u32*)nlist_dev;  // list length written by an earlier kernel
     long long emits = 0, created = 0, xapps = 0;
-    for (u32 gi = blockIdx.x; gi < nlist; gi += gridDim.x) {
+    // Groups differ in cost by orders of magnitude: after its first group a
+    // block takes the next unclaimed one (bp.fetch) rather than striding.
+    __shared__ u32 big_next;
+    auto next_group = [&](u32 g) -> u32 {
+        if (!bp.fetch) return g + gridDim.x;
+        __syncthreads();
+        if (threadIdx.x == 0) big_next = gridDim.x + atomicAdd(bp.fetch, 1u);
+        __syncthreads();
+        return big_next;
+    };
+    for (u32 gi = blockIdx.x; gi < nlist; gi = next_group(gi)) {
         OCHK(gi < sc.cap_in, 8, gi, nlist, 0)
         const u32 rep = list[gi];
         OCHK(rep < sc.cap_in, 9, rep, gi, nlist)
@@ -1036,8 +1072,9 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                         const BatchGate Gt = a.gates[t];
                         double gc, gs;
                         gate_cs(a, Gt, t, inst, gc, gs);
+                        const bool unit = !CPLX && (gs == 1.0 || gs == -1.0);
                         for (u32 m = lane; m < cnt0; m += 32)
-                            big_member<NW, CPLX, SM, REC>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits,
+                            big_member<NW, CPLX, SM, REC>(G, rcap, m, cnt0, t, Gt, gc, gs, unit, a, ctr, g_emits,
                                                            g_created, g_xapps);
                         __syncwarp();
                         cnt0 += *(volatile u32*)ctr;
@@ -1072,9 +1109,10 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                     const BatchGate Gt = a.gates[t];
                     double gc, gs;
                     gate_cs(a, Gt, t, inst, gc, gs);
+                    const bool unit = !CPLX && (gs == 1.0 || gs == -1.0);
                     for (u32 m = threadIdx.x; m < cnt0; m += blockDim.x)
-                        big_member<NW, CPLX, SM, REC>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits, g_created,
-                                                       g_xapps);
+                        big_member<NW, CPLX, SM, REC>(G, rcap, m, cnt0, t, Gt, gc, gs, unit, a, ctr, g_emits,
+                                                       g_created, g_xapps);
                     __syncthreads();
                     cnt0 += *(volatile u32*)ctr;
                     stop = *(volatile u32*)G.flag != 0;
