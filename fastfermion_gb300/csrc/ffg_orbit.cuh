@@ -893,14 +893,14 @@ constexpr size_t block_table_bytes() {
 // lower index of the two does the update), or creates K (index cnt0 + the
 // gate's creation count *ctr) when the degree filter admits it; the
 // reference's arithmetic, filter and creation rule (src/pauli/propagate.h:71-89).
-template <int NW, bool CPLX, bool SM, bool REC>
+// UNIT: the gate's |sin theta| is 1 (partners by sign flip, rot_partner_unit).
+template <int NW, bool CPLX, bool SM, bool REC, bool UNIT>
 __device__ __forceinline__ void big_member(const BigRegion<2 * NW, CPLX>& G, u32 rcap, u32 m, u32 cnt0, int t,
-                                           const BatchGate& Gt, double gc, double gs, bool unit,
-                                           const OrbitBatchArgs& a, u32* ctr, u32& g_emits, u32& g_created,
-                                           u32& g_xapps) {
+                                           const BatchGate& Gt, double gc, double gs, const OrbitBatchArgs& a,
+                                           u32* ctr, u32& g_emits, u32& g_created, u32& g_xapps) {
     constexpr int KW = 2 * NW;
     auto partner = [&](cplx b, int j) {
-        return unit ? rot_partner_unit<CPLX>(b, gs, j) : rot_partner<CPLX>(b, gs, j);
+        return UNIT ? rot_partner_unit<CPLX>(b, gs, j) : rot_partner<CPLX>(b, gs, j);
     };
     u64 q[KW], k[KW];
 #pragma unroll
@@ -1072,10 +1072,15 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                         const BatchGate Gt = a.gates[t];
                         double gc, gs;
                         gate_cs(a, Gt, t, inst, gc, gs);
-                        const bool unit = !CPLX && (gs == 1.0 || gs == -1.0);
-                        for (u32 m = lane; m < cnt0; m += 32)
-                            big_member<NW, CPLX, SM, REC>(G, rcap, m, cnt0, t, Gt, gc, gs, unit, a, ctr, g_emits,
-                                                           g_created, g_xapps);
+                        if (!CPLX && (gs == 1.0 || gs == -1.0)) {
+                            for (u32 m = lane; m < cnt0; m += 32)
+                                big_member<NW, CPLX, SM, REC, true>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits,
+                                                                     g_created, g_xapps);
+                        } else {
+                            for (u32 m = lane; m < cnt0; m += 32)
+                                big_member<NW, CPLX, SM, REC, false>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits,
+                                                                      g_created, g_xapps);
+                        }
                         __syncwarp();
                         cnt0 += *(volatile u32*)ctr;
                         gi++;
@@ -1109,10 +1114,15 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                     const BatchGate Gt = a.gates[t];
                     double gc, gs;
                     gate_cs(a, Gt, t, inst, gc, gs);
-                    const bool unit = !CPLX && (gs == 1.0 || gs == -1.0);
-                    for (u32 m = threadIdx.x; m < cnt0; m += blockDim.x)
-                        big_member<NW, CPLX, SM, REC>(G, rcap, m, cnt0, t, Gt, gc, gs, unit, a, ctr, g_emits,
-                                                       g_created, g_xapps);
+                    if (!CPLX && (gs == 1.0 || gs == -1.0)) {
+                        for (u32 m = threadIdx.x; m < cnt0; m += blockDim.x)
+                            big_member<NW, CPLX, SM, REC, true>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits,
+                                                                 g_created, g_xapps);
+                    } else {
+                        for (u32 m = threadIdx.x; m < cnt0; m += blockDim.x)
+                            big_member<NW, CPLX, SM, REC, false>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits,
+                                                                  g_created, g_xapps);
+                    }
                     __syncthreads();
                     cnt0 += *(volatile u32*)ctr;
                     stop = *(volatile u32*)G.flag != 0;
