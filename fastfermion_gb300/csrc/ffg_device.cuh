@@ -204,6 +204,25 @@ __device__ __forceinline__ cplx rot_add(cplx a, cplx b) {
     return {__dadd_rn(a.re, b.re), 0.0};
 }
 
+// GB300 runs FP64 instructions at a small fraction of the FP32 rate, and the
+// orbit kernels meet a burst of them after every gate barrier; these tests
+// therefore run on the integer pipes, on IEEE bit patterns (non-negative
+// doubles order like their bit patterns).
+// |s| == 1 exactly.
+__device__ __forceinline__ bool unit_sine(double s) {
+    return ((unsigned long long)__double_as_longlong(s) & 0x7fffffffffffffffull) == 0x3ff0000000000000ull;
+}
+// fabs(x) <= tau, with the floating-point comparison's result for every x
+// and tau (false when either is NaN; tau = -0 admits only zeros).
+__device__ __forceinline__ bool abs_le_bits(double x, double tau) {
+    const unsigned long long ax = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    const unsigned long long t = (unsigned long long)__double_as_longlong(tau);
+    const unsigned long long at = t & 0x7fffffffffffffffull;
+    if (ax > 0x7ff0000000000000ull || at > 0x7ff0000000000000ull) return false;
+    if (t >> 63) return ax == 0 && at == 0;
+    return ax <= at;
+}
+
 // The partner value when |s| = 1 (sin theta = +-1, e.g. RZZ(-pi/2)), real
 // mode: b*s is exact, so the product is b with its sign flipped when s < 0,
 // then the sign of i^j as in rot_partner -- the same value with no FP64

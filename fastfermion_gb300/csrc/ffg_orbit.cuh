@@ -248,7 +248,7 @@ __device__ __forceinline__ void gate_cs(const OrbitBatchArgs& a, const BatchGate
 template <int NW, bool CPLX>
 __device__ __forceinline__ bool survives(const u64* key, cplx c, const OrbitBatchArgs& a) {
     if (a.thr) {
-        const bool small = CPLX ? abs_le(c.re, c.im, a.tau) : (fabs(c.re) <= a.tau);
+        const bool small = CPLX ? abs_le(c.re, c.im, a.tau) : abs_le_bits(c.re, a.tau);
         if (small) return false;
     }
     if (a.max_xweight >= 0) {
@@ -677,7 +677,7 @@ __global__ void __launch_bounds__(32 * kOrbitWarps, 4) orbit_process(StoreView i
                 const BatchGate G = a.gates[t];
                 double gc, gs;
                 gate_cs(a, G, t, inst, gc, gs);
-                const bool unit = !CPLX && (gs == 1.0 || gs == -1.0);
+                const bool unit = !CPLX && unit_sine(gs);
                 auto partner = [&](cplx b, int jj) {
                     return unit ? rot_partner_unit<CPLX>(b, gs, jj) : rot_partner<CPLX>(b, gs, jj);
                 };
@@ -1072,7 +1072,7 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                         const BatchGate Gt = a.gates[t];
                         double gc, gs;
                         gate_cs(a, Gt, t, inst, gc, gs);
-                        if (!CPLX && (gs == 1.0 || gs == -1.0)) {
+                        if (!CPLX && unit_sine(gs)) {
                             for (u32 m = lane; m < cnt0; m += 32)
                                 big_member<NW, CPLX, SM, REC, true>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits,
                                                                      g_created, g_xapps);
@@ -1114,7 +1114,7 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                     const BatchGate Gt = a.gates[t];
                     double gc, gs;
                     gate_cs(a, Gt, t, inst, gc, gs);
-                    if (!CPLX && (gs == 1.0 || gs == -1.0)) {
+                    if (!CPLX && unit_sine(gs)) {
                         for (u32 m = threadIdx.x; m < cnt0; m += blockDim.x)
                             big_member<NW, CPLX, SM, REC, true>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits,
                                                                  g_created, g_xapps);
