@@ -231,7 +231,7 @@ template <bool CPLX>
 __device__ __forceinline__ cplx rot_partner_unit(cplx b, double s, int j) {
     if (CPLX) return rot_partner<true>(b, s, j);
     if (!(j & 1)) return {0.0, 0.0};
-    const bool neg = (s < 0.0) != ((j & 3) == 1);
+    const bool neg = ((unsigned long long)__double_as_longlong(s) >> 63) != (unsigned long long)((j & 3) == 1);
     return {__longlong_as_double(__double_as_longlong(b.re) ^ (neg ? (long long)0x8000000000000000ull : 0ll)), 0.0};
 }
 

@@ -468,7 +468,7 @@ constexpr int kMSubWarps = 8;     // sub-warp tier: warps per block
 // groups whose orbit bound m0 * 2^|A| is at most 64 (they cannot outgrow the
 // table); the others go to sc.list2 for the warp tier.
 template <int KW>
-__global__ void __launch_bounds__(32 * kMSubWarps) morbit_sub(StoreView in, StoreView out, OrbitScratch sc,
+__global__ void __launch_bounds__(32 * kMSubWarps, 2) morbit_sub(StoreView in, StoreView out, OrbitScratch sc,
                                                             OrbitCounters* oc, MOrbitArgs a) {
     wait_prior_grid();
     extern __shared__ __align__(16) unsigned char msm[];
@@ -507,7 +507,7 @@ constexpr u32 kMTeamCap = 1024;   // team tier (256 threads)
 // Warp tier: one warp per group, tables in shared memory; groups that do not
 // fit (or have route_big or more gates) are listed in sc.big.
 template <int KW>
-__global__ void __launch_bounds__(32 * kMWarps) morbit_warp(StoreView in, StoreView out, OrbitScratch sc,
+__global__ void __launch_bounds__(32 * kMWarps, 2) morbit_warp(StoreView in, StoreView out, OrbitScratch sc,
                                                           OrbitCounters* oc, MOrbitArgs a) {
     wait_prior_grid();
     extern __shared__ __align__(16) unsigned char msm[];

@@ -554,24 +554,21 @@ struct OrbitTable {
     unsigned int flag;                    // the group outgrew the table
 };
 
-// Hash of a key for the per-group tables (one evaluation per member and gate,
-// so it is kept short): the key words are folded into 64 bits with a
-// different rotation per word (the x and z bits of one qubit land apart),
-// the high half is folded into the low one, and one multiplication by an odd
-// constant mixes it (multiplicative hashing).  Bits 32.. of the product, the
-// table position, depend on every bit of the fold; bits 13..31 serve as a
-// fingerprint.  A full key match is still required to find a member, so the
-// hash only decides where members sit in a table, never the results.
-__device__ __forceinline__ u64 rotl64(u64 x, int r) { return (x << r) | (x >> (64 - r)); }
-
+// Hash of a key for the per-group tables: a chain of 64-bit mixing rounds
+// over the key words, so that every bit of every word reaches every bit of
+// the result.  Bits 32.. are the table position, bits 13..31 a fingerprint;
+// the hash is computed once per member and gate and reused by the insert.
+// (Shorter hashes that first fold the words into 64 bits by XOR map keys
+// that differ on particular qubit pairs to the same value; on the large
+// W = 10 groups that lengthened the probe chains and slowed the workload by a
+// third.)  A full key match is still required to find a member, so the hash
+// only decides where members sit in a table, never the results.
 template <int KW>
 __device__ __forceinline__ u64 tab_hash(const u64* k) {
-    constexpr int rot[4] = {0, 32, 16, 48};
-    u64 x = k[0];
+    u64 h = mix64(k[0] ^ 0x2545f4914f6cdd1dull);
 #pragma unroll
-    for (int w = 1; w < KW; w++) x ^= rotl64(k[w], rot[w & 3]);
-    x ^= x >> 32;
-    return x * 0x9e3779b97f4a7c15ull;
+    for (int w = 1; w < KW; w++) h = mix64(h ^ k[w]);
+    return h;
 }
 __device__ __forceinline__ u32 tab_pos(u64 h) { return (u32)(h >> 32); }
 __device__ __forceinline__ u32 tab_fp(u64 h) { return (u32)h >> 13; }  // 19 bits
@@ -966,23 +963,19 @@ __device__ __forceinline__ void big_member(const BigRegion<2 * NW, CPLX>& G, u32
     }
 }
 
-// Groups that start with at most this many members are first run by one warp
-// of the block (see orbit_process_big).
-constexpr u32 kWarpPhase = 64;
 
 // Block-level group processing with TB threads per block.  SM: the table lives
 // in dynamic shared memory (CAP members); otherwise in the block's
 // global-memory region of bp.
 template <int NW, bool CPLX, bool SM, int TB = 1024, u32 CAP = kBlockCap, bool REC = false>
-__global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView out, OrbitScratch sc,
+__global__ void __launch_bounds__(TB, TB <= 256 ? 4 : 1) orbit_process_big(StoreView in, StoreView out, OrbitScratch sc,
                                                           OrbitCounters* oc, OrbitBatchArgs a, BigPool bp,
                                                           const u32* list, u32 nlist, const u32* nlist_dev) {
     wait_prior_grid();
     constexpr int KW = 2 * NW;
     static_assert(!SM || CAP <= (1u << kFpShift), "member indexes of a shared-memory table fit beside the fingerprint");
     __shared__ long long red[3][32];
-    __shared__ u32 big_cr[3];    // members created by a gate (ring of three)
-    __shared__ u32 big_done[2];  // gates applied and members after the warp phase
+    __shared__ u32 big_cr[3];  // members created by a gate (ring of three)
     extern __shared__ __align__(16) unsigned char btab[];
     if (*(volatile u32*)&oc->skip) return;
     if (nlist_dev) nlist = *(volatile const u32*)nlist_dev;  // list length written by an earlier kernel
@@ -1054,51 +1047,8 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
         const u32 inst = group_instance(in, a, rep);
         const u64* A = sc.amask + rep;  // word w of the group's gate set at A[w * cap_in]
         u32 cnt0 = m0;   // members before the current gate (the same in every thread)
-        int done = 0;    // gates of A applied so far
-        // Warp phase: while the group has at most kWarpPhase members, warp 0
-        // alone applies the gates (warp barriers only); the block's other warps
-        // wait at one block barrier.
-        if (SM && cnt0 <= kWarpPhase) {
-            if (threadIdx.x < 32) {
-                const int lane = threadIdx.x;
-                int gi = 0;
-                for (int wd = 0; wd < kAW && cnt0 <= kWarpPhase; wd++) {
-                    u64 bits = A[(u64)wd * sc.cap_in];
-                    while (bits && cnt0 <= kWarpPhase) {
-                        const int t = 64 * wd + __ffsll((long long)bits) - 1;
-                        bits &= bits - 1;
-                        u32* ctr = &big_cr[gi % 3];
-                        if (lane == 0) big_cr[(gi + 1) % 3] = 0;
-                        const BatchGate Gt = a.gates[t];
-                        double gc, gs;
-                        gate_cs(a, Gt, t, inst, gc, gs);
-                        if (!CPLX && unit_sine(gs)) {
-                            for (u32 m = lane; m < cnt0; m += 32)
-                                big_member<NW, CPLX, SM, REC, true>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits,
-                                                                     g_created, g_xapps);
-                        } else {
-                            for (u32 m = lane; m < cnt0; m += 32)
-                                big_member<NW, CPLX, SM, REC, false>(G, rcap, m, cnt0, t, Gt, gc, gs, a, ctr, g_emits,
-                                                                      g_created, g_xapps);
-                        }
-                        __syncwarp();
-                        cnt0 += *(volatile u32*)ctr;
-                        gi++;
-                        if (*(volatile u32*)G.flag) break;
-                    }
-                    if (*(volatile u32*)G.flag) break;
-                }
-                if (lane == 0) {
-                    big_done[0] = (u32)gi;
-                    big_done[1] = cnt0;
-                }
-            }
-            __syncthreads();
-            done = (int)big_done[0];
-            cnt0 = big_done[1];
-        }
-        // Block phase: every thread, one block barrier per gate.  Creations of
-        // gate i count in big_cr[i % 3]; the slot of gate i + 1 is cleared
+        // Gates in order, every thread, one block barrier per gate.  Creations
+        // of gate i count in big_cr[i % 3]; the slot of gate i + 1 is cleared
         // during gate i (its last readers passed the barrier of gate i - 1).
         {
             int gi = 0;
@@ -1108,8 +1058,7 @@ __global__ void __launch_bounds__(TB) orbit_process_big(StoreView in, StoreView 
                 while (bits && !stop) {
                     const int t = 64 * wd + __ffsll((long long)bits) - 1;
                     bits &= bits - 1;
-                    if (gi++ < done) continue;
-                    u32* ctr = &big_cr[(gi - 1) % 3];
+                    u32* ctr = &big_cr[gi++ % 3];
                     if (threadIdx.x == 0) big_cr[gi % 3] = 0;
                     const BatchGate Gt = a.gates[t];
                     double gc, gs;
