@@ -6,7 +6,8 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libffg.so")
-SOURCES = ["ffg_engine.cu", "ffg_noalloc.cu", "ffg_sortmerge.cu", "ffg_mlp.cu"]
+SOURCES = ["ffg_engine.cu", "ffg_pauli.cu", "ffg_majorana.cu", "ffg_batch.cu", "ffg_convert.cu", "ffg_noalloc.cu",
+           "ffg_sortmerge.cu", "ffg_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

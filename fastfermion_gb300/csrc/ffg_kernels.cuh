@@ -13,6 +13,9 @@
 // is owned by the thread of its lower store position, so the update is done in
 // place without atomics on coefficients, and each coefficient sees exactly the
 // one rounding per operation that the reference applies.
+// The kernel headers are included by several translation units of libffg:
+// templates and inline functions may repeat across them, and the few
+// non-template kernels are declared static (internal linkage).
 #pragma once
 #include "ffg_device.cuh"
 
@@ -404,7 +407,7 @@ __global__ void __launch_bounds__(kBlock) clifford_kernel(StoreView s, DevCounte
 // ---------------------------------------------------------------------------
 // index maintenance
 // ---------------------------------------------------------------------------
-__global__ void clear_slots_kernel(u64* slots, u64 nslots) {
+static __global__ void clear_slots_kernel(u64* slots, u64 nslots) {
     const u64 stride = (u64)gridDim.x * blockDim.x;
     for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += stride) slots[i] = kEmptySlot;
 }
@@ -429,7 +432,7 @@ __global__ void __launch_bounds__(kBlock) index_kernel(StoreView s, DevCounters*
 // ---------------------------------------------------------------------------
 constexpr int kTileItems = kBlock * 8;
 
-__global__ void __launch_bounds__(kBlock) tile_count_kernel(StoreView s, DevCounters* C, u64* counts) {
+static __global__ void __launch_bounds__(kBlock) tile_count_kernel(StoreView s, DevCounters* C, u64* counts) {
     const u64 n = *(volatile u64*)&C->n;
     const u64 ntiles = (n + kTileItems - 1) / kTileItems;
     __shared__ int red[kBlock / 32];
@@ -452,7 +455,7 @@ __global__ void __launch_bounds__(kBlock) tile_count_kernel(StoreView s, DevCoun
 }
 
 // exclusive scan of the tile counts (one block); writes the live total
-__global__ void __launch_bounds__(1024) tile_scan_kernel(DevCounters* C, u64* counts) {
+static __global__ void __launch_bounds__(1024) tile_scan_kernel(DevCounters* C, u64* counts) {
     const u64 n = *(volatile u64*)&C->n;
     const u64 ntiles = (n + kTileItems - 1) / kTileItems;
     __shared__ u64 carry;
@@ -528,7 +531,7 @@ __global__ void __launch_bounds__(kBlock) scatter_kernel(StoreView src, StoreVie
     }
 }
 
-__global__ void compact_commit_kernel(DevCounters* C, const u64* counts) {
+static __global__ void compact_commit_kernel(DevCounters* C, const u64* counts) {
     volatile DevCounters* V = C;
     const u64 n = V->n;
     const u64 ntiles = (n + kTileItems - 1) / kTileItems;
@@ -604,7 +607,7 @@ __global__ void __launch_bounds__(kBlock) expect_kernel(StoreView s, u64 n, int 
     }
 }
 
-__global__ void expect_final_kernel(const double* part_re, const double* part_im, int nparts, double* out) {
+static __global__ void expect_final_kernel(const double* part_re, const double* part_im, int nparts, double* out) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         double a = 0.0, b = 0.0;
         for (int i = 0; i < nparts; i++) {
@@ -669,7 +672,7 @@ __global__ void __launch_bounds__(kBlock) topk_cut_kernel(StoreView s, DevCounte
     kernel_exit(C, e, d_alive, sh, false);
 }
 
-__global__ void kill_list_kernel(StoreView s, DevCounters* C, const u64* list, u64 m) {
+static __global__ void kill_list_kernel(StoreView s, DevCounters* C, const u64* list, u64 m) {
     for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (u64)gridDim.x * blockDim.x)
         s.dead[list[t]] = 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) {

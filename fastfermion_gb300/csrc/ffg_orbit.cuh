@@ -323,7 +323,7 @@ __device__ __forceinline__ void out_append(const StoreView& o, OrbitCounters* oc
 // and clears the two retry counts.  Otherwise the batch is marked skipped and
 // every kernel of it returns at once, leaving the scratch as the incomplete
 // batch left it.
-__global__ void orbit_gate(OrbitCounters* cur, const OrbitCounters* prev, u64 n_first, u64 gslots_cap,
+static __global__ void orbit_gate(OrbitCounters* cur, const OrbitCounters* prev, u64 n_first, u64 gslots_cap,
                            u32* nretry) {
     wait_prior_grid();
     constexpr u32 nw = sizeof(OrbitCounters) / 4;
@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(kBlock) orbit_group(OrbitScratch sc, OrbitCoun
 // first member position of every group (groups listed in sc.groups).  Any
 // placement of the groups works (each group is processed on its own), so the
 // ranges come from warp-aggregated atomic additions, in parallel.
-__global__ void __launch_bounds__(kBlock) orbit_offsets(OrbitScratch sc, OrbitCounters* oc) {
+static __global__ void __launch_bounds__(kBlock) orbit_offsets(OrbitScratch sc, OrbitCounters* oc) {
     wait_prior_grid();
     if (*(volatile u32*)&oc->skip) return;
     const u32 ng = *(volatile u32*)&oc->ngroups;

@@ -53,7 +53,7 @@ __device__ __forceinline__ void jw_string(const u64 (&a)[4], u64 (&x)[2], u64 (&
 
 // keys: kw planes (stride n) of Majorana strings; out: 4 Pauli planes (stride
 // n).  keep[i] = 0 when the mapped coefficient is exactly zero.
-__global__ void __launch_bounds__(kBlock) jw_kernel(const u64* mkeys, int kw, const double* re, const double* im,
+static __global__ void __launch_bounds__(kBlock) jw_kernel(const u64* mkeys, int kw, const double* re, const double* im,
                                                     u64 n, u64* pkeys, double* ore, double* oim,
                                                     unsigned char* keep) {
     const u64 stride = (u64)gridDim.x * blockDim.x;
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kBlock) jw_kernel(const u64* mkeys, int kw, co
 // term t has the bit-reversed Z mask zf[t] and coefficient i^{#Y} c = (cr, ci).
 // pass 0 counts the nonzero entries of every column, pass 1 writes them at
 // colptr[b] (row indices and values).
-__global__ void __launch_bounds__(kBlock) sparse_kernel(u64 ncols, const u64* gxf, const u32* gstart, u32 ngroups,
+static __global__ void __launch_bounds__(kBlock) sparse_kernel(u64 ncols, const u64* gxf, const u32* gstart, u32 ngroups,
                                                         const u64* zf, const double* cr, const double* ci,
                                                         long long* colcount, const long long* colptr,
                                                         long long* rows, double* vre, double* vim, int pass) {
