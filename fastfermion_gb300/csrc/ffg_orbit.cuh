@@ -806,9 +806,9 @@ struct BigRegion {
     u64* key;      // [KW][rcap]
     double* re;
     double* im;
-    u32* slot;     // [2*rcap], 0xffffffff = empty
-    u32* cnt;
-    u32* flag;
+    u32* slot;     // [2*rcap], 0xffffffff = empty; (fingerprint << 12) | member in shared memory
+    u32* cnt;      // members when the group was loaded (the kernel keeps the running count in registers)
+    u32* flag;     // the group outgrew the table
 };
 
 template <int KW, bool CPLX>
