@@ -554,21 +554,29 @@ struct OrbitTable {
     unsigned int flag;                    // the group outgrew the table
 };
 
-// Hash of a key for the per-group tables: a chain of 64-bit mixing rounds
-// over the key words, so that every bit of every word reaches every bit of
-// the result.  Bits 32.. are the table position, bits 13..31 a fingerprint;
-// the hash is computed once per member and gate and reused by the insert.
-// (Shorter hashes that first fold the words into 64 bits by XOR map keys
-// that differ on particular qubit pairs to the same value; on the large
-// W = 10 groups that lengthened the probe chains and slowed the workload by a
+// Hash of a key for the per-group tables, on the critical path of every
+// member update: each key word is multiplied by its own odd constant (the
+// four products are independent), the products are rotated apart and XORed
+// (a multiplication carries into higher bits only, so the rotations keep the
+// top-bit flips of different words from cancelling), and one 64-bit mixing
+// round spreads the result.  Bits 32.. are the table position, bits 13..31 a
+// fingerprint; the hash is computed once per member and gate and reused by
+// the insert.  (Hashes that first fold the key words by XOR map keys that
+// differ on particular qubit pairs to the same value; on the large W = 10
+// groups that lengthened the probe chains and slowed the workload by a
 // third.)  A full key match is still required to find a member, so the hash
 // only decides where members sit in a table, never the results.
+__device__ __forceinline__ u64 rotl64(u64 x, int r) { return r ? (x << r) | (x >> (64 - r)) : x; }
+
 template <int KW>
 __device__ __forceinline__ u64 tab_hash(const u64* k) {
-    u64 h = mix64(k[0] ^ 0x2545f4914f6cdd1dull);
+    constexpr u64 mul[4] = {0x9e3779b97f4a7c15ull, 0xc2b2ae3d27d4eb4full, 0x165667b19e3779f9ull,
+                            0xd6e8feb86659fd93ull};
+    constexpr int rot[4] = {0, 17, 31, 47};
+    u64 x = k[0] * mul[0];
 #pragma unroll
-    for (int w = 1; w < KW; w++) h = mix64(h ^ k[w]);
-    return h;
+    for (int w = 1; w < KW; w++) x ^= rotl64(k[w] * mul[w & 3], rot[w & 3]);
+    return mix64(x);
 }
 __device__ __forceinline__ u32 tab_pos(u64 h) { return (u32)(h >> 32); }
 __device__ __forceinline__ u32 tab_fp(u64 h) { return (u32)h >> 13; }  // 19 bits
