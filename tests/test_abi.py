@@ -31,6 +31,14 @@ def test_header_symbols_exported():
         assert hasattr(L, s)
 
 
+def test_every_translation_unit_is_built():
+    """Every CUDA source of the library is compiled into libffg (the host engine
+    is split by entry point over ffg_engine_impl.cuh)."""
+    csrc = os.path.join(ROOT, "fastfermion_gb300", "csrc")
+    units = sorted(f for f in os.listdir(csrc) if f.endswith(".cu"))
+    assert units == sorted(_build.SOURCES), (units, _build.SOURCES)
+
+
 def test_binding_covers_header():
     assert sorted(_native.EXPORTS) == declared()
 
